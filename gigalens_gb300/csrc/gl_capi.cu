@@ -1,0 +1,579 @@
+// Host side of the C ABI: plan construction (validation, PSF+binning
+// sub-kernels, coordinate grid, device constants) and the compute entry
+// points.  No compute happens here; every entry point enqueues kernels.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "gl_internal.cuh"
+
+namespace gl {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+static int cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? GL_ERR_NOMEM : GL_ERR_CUDA;
+  }
+  return GL_OK;
+}
+
+static int param_count(int type) {
+  switch (type) {
+    case GL_PROF_EPL: return 6;
+    case GL_PROF_SHEAR: return 2;
+    case GL_PROF_SIS: return 3;
+    case GL_PROF_SIE: return 5;
+    case GL_PROF_SERSIC: return 5;
+    case GL_PROF_SERSIC_ELLIPSE: return 7;
+    case GL_PROF_SHAPELETS: return 3;
+    default: return -1;
+  }
+}
+
+// Map the model descriptor to a compiled family of the fused kernel and
+// resolve every slot to flat-vector columns.  SERSIC (spherical) runs as
+// SERSIC_ELLIPSE with e1 = e2 = 0.
+static int resolve_family(const gl_model_desc* m, int* family, DevProfile* epl, DevProfile* shear,
+                          DevProfile* llight, DevProfile* source) {
+  int n_epl = 0, n_shear = 0, n_ll = 0, n_src = 0;
+  for (auto* p : {epl, shear, llight, source}) {
+    p->type = GL_PROF_NONE;
+    p->niter = 0;
+    for (int i = 0; i < GL_MAX_PROFILE_PARAMS; ++i) p->col[i] = -1;
+  }
+  for (int i = 0; i < m->n_profiles; ++i) {
+    const gl_profile_desc& p = m->prof[i];
+    if (p.group == GL_GROUP_LENS) {
+      if (p.type == GL_PROF_EPL) {
+        ++n_epl;
+        epl->type = p.type;
+        epl->niter = p.niter;
+        for (int k = 0; k < 6; ++k) epl->col[k] = p.col[k];
+      } else if (p.type == GL_PROF_SHEAR) {
+        ++n_shear;
+        shear->type = p.type;
+        for (int k = 0; k < 2; ++k) shear->col[k] = p.col[k];
+      } else {
+        set_error("fused model: lens profile type %d is not supported (EPL, SHEAR)", p.type);
+        return GL_ERR_UNSUPPORTED;
+      }
+    } else if (p.group == GL_GROUP_LENS_LIGHT || p.group == GL_GROUP_SOURCE) {
+      DevProfile* dst = p.group == GL_GROUP_LENS_LIGHT ? llight : source;
+      int* cnt = p.group == GL_GROUP_LENS_LIGHT ? &n_ll : &n_src;
+      ++*cnt;
+      dst->type = GL_PROF_SERSIC_ELLIPSE;
+      if (p.type == GL_PROF_SERSIC_ELLIPSE) {
+        for (int k = 0; k < 7; ++k) dst->col[k] = p.col[k];
+      } else if (p.type == GL_PROF_SERSIC) {
+        // R_sersic, n_sersic, center_x, center_y, Ie -> SE slots 0,1,4,5,6
+        dst->col[0] = p.col[0];
+        dst->col[1] = p.col[1];
+        dst->col[4] = p.col[2];
+        dst->col[5] = p.col[3];
+        dst->col[6] = p.col[4];
+      } else {
+        set_error("fused model: light profile type %d is not supported (SERSIC, SERSIC_ELLIPSE)",
+                  p.type);
+        return GL_ERR_UNSUPPORTED;
+      }
+      if (p.use_lstsq) dst->col[6] = -1;   // unit amplitude
+    } else {
+      set_error("profile %d: bad group %d", i, p.group);
+      return GL_ERR_INVALID;
+    }
+  }
+  if (n_epl != 1 || n_shear > 1 || n_ll > 1 || n_src != 1) {
+    set_error("fused model needs one EPL, at most one SHEAR, at most one lens light and one source "
+              "light profile (got %d, %d, %d, %d)", n_epl, n_shear, n_ll, n_src);
+    return GL_ERR_UNSUPPORTED;
+  }
+  if (epl->niter < 0 || epl->niter > kMaxTerms) {
+    set_error("EPL niter %d outside [0, %d]", epl->niter, kMaxTerms);
+    return GL_ERR_UNSUPPORTED;
+  }
+  if (n_shear) *family = n_ll ? FAM_EPL_SHEAR_SE_SE : FAM_EPL_SHEAR_SE;
+  else *family = n_ll ? FAM_EPL_SE_SE : FAM_EPL_SE;
+  return GL_OK;
+}
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+struct HostImage {
+  std::vector<float> obs, grid, kern;
+};
+
+// Fill the device-ready description of one image; host arrays go to hi.
+static int build_image(const gl_image_desc& g, DevImage& I, HostImage& hi) {
+  const int N = g.num_pix, ss = g.supersample;
+  if (N <= 0 || N > 4096) {
+    set_error("num_pix %d out of range", N);
+    return GL_ERR_INVALID;
+  }
+  if (ss < 1 || ss > 2) {
+    set_error("supersample %d: the fused kernel supports 1 and 2", ss);
+    return GL_ERR_UNSUPPORTED;
+  }
+  if (g.kernel_size < 0 || (g.kernel_size > 0 && (g.kernel_size % 2 == 0 || !g.kernel))) {
+    set_error("kernel_size %d must be 0 or odd with a kernel pointer", g.kernel_size);
+    return GL_ERR_INVALID;
+  }
+  if (!(g.exp_time > 0.f) || !(g.background_rms >= 0.f)) {
+    set_error("exp_time must be > 0 and background_rms >= 0");
+    return GL_ERR_INVALID;
+  }
+  memset(&I, 0, sizeof(I));
+  I.N = N;
+  I.ss = ss;
+  I.nplanes = ss * ss;
+  // flipped PSF (the reference correlates with kernel[::-1, ::-1])
+  const int k = g.kernel_size > 0 ? g.kernel_size : 1;
+  std::vector<double> flat(k * k, 1.0);
+  if (g.kernel_size > 0)
+    for (int m = 0; m < k; ++m)
+      for (int n = 0; n < k; ++n) flat[m * k + n] = g.kernel[(k - 1 - m) * k + (k - 1 - n)];
+  const int pad = (k - 1) / 2;
+  const int kc = k + ss - 1;
+  // combined kernel: correlation with PSF then ss x ss average pooling
+  std::vector<double> Kc(kc * kc, 0.0);
+  for (int u = 0; u < kc; ++u)
+    for (int v = 0; v < kc; ++v) {
+      double s = 0.0;
+      for (int a = 0; a < ss; ++a)
+        for (int b = 0; b < ss; ++b) {
+          int m = u - a, n = v - b;
+          if (m >= 0 && m < k && n >= 0 && n < k) s += flat[m * k + n];
+        }
+      Kc[u * kc + v] = s / (ss * ss);
+    }
+  const int KS = (kc + ss - 1) / ss;
+  if (KS > kMaxKS) {
+    set_error("PSF too large for the fused kernel: sub-kernel side %d > %d", KS, kMaxKS);
+    return GL_ERR_UNSUPPORTED;
+  }
+  if (KS % 2 == 0) {
+    set_error("PSF size %d with supersample %d gives an even sub-kernel (%d); not supported", k, ss,
+              KS);
+    return GL_ERR_UNSUPPORTED;
+  }
+  I.KS = KS;
+  I.ksp = (KS + 3) & ~3;
+  for (int p = 0; p < ss; ++p) I.d[p] = (p + pad) / ss;
+  for (int p = 1; p < ss; ++p)
+    if ((I.d[p] - I.d[0]) % 4 != 0) {
+      set_error("PSF size %d with supersample %d: unaligned parity offsets; not supported", k, ss);
+      return GL_ERR_UNSUPPORTED;
+    }
+  hi.kern.assign(I.nplanes * KS * I.ksp, 0.f);
+  for (int p = 0; p < ss; ++p)
+    for (int q = 0; q < ss; ++q)
+      for (int m = 0; m < KS; ++m)
+        for (int l = 0; l < KS; ++l) {
+          int u = ss * m + (p + pad) % ss, v = ss * l + (q + pad) % ss;
+          double val = (u < kc && v < kc) ? Kc[u * kc + v] : 0.0;
+          hi.kern[((p * ss + q) * KS + m) * I.ksp + l] = (float)val;
+        }
+  // shared-memory layout
+  I.ncb = ((N + kColBlock - 1) / kColBlock + 3) & ~3;
+  I.rows2 = (N + 1) & ~1;
+  const int segn = (kColBlock + KS - 1 + 3) & ~3;
+  int pitch = (int)align_up(kColBlock * (I.ncb - 1) + segn, 4);
+  if ((pitch / 4) % 2 == 0) pitch += 4;
+  for (int q = 0; q < ss; ++q) I.padI[q] = I.d[q];
+  I.pitchI = pitch;
+  I.padW = KS - 1 - I.d[0];
+  I.pitchW = pitch;
+  I.offI = 0;
+  I.offW = I.nplanes * N * I.pitchI;
+  I.offK = I.offW + N * I.pitchW;
+  I.smem_floats = I.offK + I.nplanes * KS * I.ksp;
+  // coordinate grid, gigalens/simulator.py:91-125 (float64 then float32)
+  const int S = ss * N;
+  double T[4];
+  for (int i = 0; i < 4; ++i) T[i] = (double)g.transform_pix2angle[i] / ss;
+  // lo = min(arange(S) - mean) and the origin T @ [lo, lo] are float32 in the reference
+  const float lo = 0.f - (float)((double)(S - 1) / 2.0);
+  const double ra0 = (double)(float)((float)((float)T[0] * lo) + (float)((float)T[1] * lo));
+  const double dec0 = (double)(float)((float)((float)T[2] * lo) + (float)((float)T[3] * lo));
+  hi.grid.assign((size_t)I.nplanes * N * N * 2, 0.f);
+  for (int p = 0; p < ss; ++p)
+    for (int q = 0; q < ss; ++q)
+      for (int Y = 0; Y < N; ++Y)
+        for (int X = 0; X < N; ++X) {
+          const double row = ss * Y + p, col = ss * X + q;
+          const size_t v = (((size_t)(p * ss + q) * N + Y) * N + X) * 2;
+          hi.grid[v] = (float)(T[0] * col + T[1] * row + ra0);
+          hi.grid[v + 1] = (float)(T[2] * col + T[3] * row + dec0);
+        }
+  I.t00 = (float)T[0];
+  I.t01 = (float)T[1];
+  I.t10 = (float)T[2];
+  I.t11 = (float)T[3];
+  I.x0 = (float)ra0;
+  I.y0 = (float)dec0;
+  I.cf = (float)((double)g.transform_pix2angle[0] * g.transform_pix2angle[3] -
+                 (double)g.transform_pix2angle[1] * g.transform_pix2angle[2]);
+  I.bg2 = g.background_rms * g.background_rms;
+  I.inv_t = 1.f / g.exp_time;
+  if (g.observed) hi.obs.assign(g.observed, g.observed + (size_t)N * N);
+  return GL_OK;
+}
+
+static int check_device(const gl_plan* plan) {
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != plan->device) {
+    set_error("plan was created on device %d but device %d is current", plan->device, dev);
+    return GL_ERR_INVALID;
+  }
+  return GL_OK;
+}
+
+static DevPriorLeaf make_leaf(const gl_prior_leaf& l) {
+  DevPriorLeaf d;
+  memset(&d, 0, sizeof(d));
+  d.dist = l.dist;
+  switch (l.dist) {
+    case GL_DIST_NORMAL:
+    case GL_DIST_LOGNORMAL:
+      d.loc = l.a;
+      d.scale = l.b;
+      break;
+    case GL_DIST_UNIFORM:
+      d.lo = l.a;
+      d.hi = l.b;
+      d.lognorm = (float)std::log((double)l.b - (double)l.a);
+      d.loglen = d.lognorm;
+      break;
+    case GL_DIST_TRUNCNORMAL: {
+      d.loc = l.a;
+      d.scale = l.b;
+      d.lo = l.c;
+      d.hi = l.d;
+      const double al = ((double)l.c - l.a) / l.b, be = ((double)l.d - l.a) / l.b;
+      const double Z = 0.5 * (std::erfc(-be / std::sqrt(2.0)) - std::erfc(-al / std::sqrt(2.0)));
+      d.lognorm = (float)std::log(Z);
+      d.loglen = (float)std::log((double)l.d - (double)l.c);
+      break;
+    }
+    default:
+      break;
+  }
+  return d;
+}
+
+static void fill_args(const gl_plan* plan, FusedArgs& a) {
+  memset(&a, 0, sizeof(a));
+  a.family = plan->family;
+  a.d = plan->model.n_params;
+  a.n_images = plan->n_images;
+  for (int i = 0; i < plan->n_images; ++i) a.img[i] = plan->img[i];
+  a.epl = plan->epl;
+  a.shear = plan->shear;
+  a.llight = plan->llight;
+  a.source = plan->source;
+  a.has_prior = plan->has_prior;
+  for (int i = 0; i < GL_MAX_PARAMS; ++i) a.prior[i] = plan->prior[i];
+  a.img_stride = plan->max_pix;
+}
+
+}  // namespace gl
+
+using namespace gl;
+
+extern "C" {
+
+int gl_abi_version(void) { return GL_ABI_VERSION; }
+
+const char* gl_last_error(void) { return g_err; }
+
+int gl_device_info(int* sm_count, int* smem_optin_bytes) {
+  int dev = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  if (sm_count) cudaDeviceGetAttribute(sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (smem_optin_bytes)
+    cudaDeviceGetAttribute(smem_optin_bytes, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return GL_OK;
+}
+
+int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int n_images,
+                   gl_plan** out) {
+  if (!model || !images || !out || n_images < 1 || n_images > GL_MAX_IMAGES) {
+    set_error("gl_plan_create: bad arguments (n_images %d)", n_images);
+    return GL_ERR_INVALID;
+  }
+  *out = nullptr;
+  if (model->n_profiles < 1 || model->n_profiles > GL_MAX_PROFILES || model->n_params < 1 ||
+      model->n_params > GL_MAX_PARAMS) {
+    set_error("gl_plan_create: bad model (n_profiles %d, n_params %d)", model->n_profiles,
+              model->n_params);
+    return GL_ERR_INVALID;
+  }
+  for (int i = 0; i < model->n_profiles; ++i) {
+    const gl_profile_desc& p = model->prof[i];
+    const int np = param_count(p.type);
+    if (np < 0) {
+      set_error("profile %d: unknown type %d", i, p.type);
+      return GL_ERR_INVALID;
+    }
+    for (int k = 0; k < np; ++k)
+      if (p.col[k] < -1 || p.col[k] >= model->n_params) {
+        set_error("profile %d parameter %d: column %d out of range", i, k, p.col[k]);
+        return GL_ERR_INVALID;
+      }
+  }
+  gl_plan* plan = new gl_plan;
+  memset(plan, 0, sizeof(*plan));
+  plan->model = *model;
+  plan->n_images = n_images;
+  int rc = resolve_family(model, &plan->family, &plan->epl, &plan->shear, &plan->llight,
+                          &plan->source);
+  if (rc) {
+    delete plan;
+    return rc;
+  }
+  rc = cuda_check(cudaGetDevice(&plan->device), "cudaGetDevice");
+  if (rc) {
+    delete plan;
+    return rc;
+  }
+  std::vector<HostImage> hi(n_images);
+  size_t bytes = 0;
+  int smem_floats = 0;
+  for (int i = 0; i < n_images; ++i) {
+    plan->host_img[i] = images[i];
+    rc = build_image(images[i], plan->img[i], hi[i]);
+    if (rc) {
+      delete plan;
+      return rc;
+    }
+    bytes += align_up(hi[i].obs.size() * 4, 256) + align_up(hi[i].grid.size() * 4, 256) +
+             align_up(hi[i].kern.size() * 4, 256);
+    if (plan->img[i].smem_floats > smem_floats) smem_floats = plan->img[i].smem_floats;
+    const int pix = images[i].num_pix * images[i].num_pix;
+    if (pix > plan->max_pix) plan->max_pix = pix;
+  }
+  int dev_smem = 0;
+  cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
+  plan->smem_bytes = smem_floats * 4;
+  const int static_smem = 8 * 1024;   // SmemStatic upper bound
+  if (plan->smem_bytes + static_smem > dev_smem) {
+    set_error("image needs %d bytes of shared memory; the device allows %d per block",
+              plan->smem_bytes + static_smem, dev_smem);
+    delete plan;
+    return GL_ERR_UNSUPPORTED;
+  }
+  rc = cuda_check(cudaMalloc((void**)&plan->dev_buf, bytes), "cudaMalloc(plan)");
+  if (rc) {
+    delete plan;
+    return rc;
+  }
+  plan->dev_buf_bytes = bytes;
+  char* base = (char*)plan->dev_buf;
+  for (int i = 0; i < n_images; ++i) {
+    DevImage& I = plan->img[i];
+    auto put = [&](const std::vector<float>& v) -> const float* {
+      if (v.empty()) return nullptr;
+      const float* p = (const float*)base;
+      cudaMemcpy((void*)p, v.data(), v.size() * 4, cudaMemcpyHostToDevice);
+      base += align_up(v.size() * 4, 256);
+      return p;
+    };
+    I.obs = put(hi[i].obs);
+    I.grid = put(hi[i].grid);
+    I.kern = put(hi[i].kern);
+  }
+  rc = cuda_check(cudaGetLastError(), "plan upload");
+  if (!rc) rc = fused_kernel_prepare(plan->smem_bytes);
+  if (rc) {
+    cudaFree(plan->dev_buf);
+    delete plan;
+    return rc;
+  }
+  *out = plan;
+  return GL_OK;
+}
+
+int gl_plan_set_prior(gl_plan* plan, const gl_prior_leaf* leaves, int n_leaves) {
+  if (!plan || !leaves || n_leaves != plan->model.n_params) {
+    set_error("gl_plan_set_prior: need one leaf per parameter (%d)", plan ? plan->model.n_params : -1);
+    return GL_ERR_INVALID;
+  }
+  for (int i = 0; i < n_leaves; ++i) {
+    const gl_prior_leaf& l = leaves[i];
+    const bool ok = (l.dist == GL_DIST_NORMAL || l.dist == GL_DIST_LOGNORMAL) ? l.b > 0.f
+                    : l.dist == GL_DIST_UNIFORM                            ? l.b > l.a
+                    : l.dist == GL_DIST_TRUNCNORMAL                        ? (l.b > 0.f && l.d > l.c)
+                                                                           : false;
+    if (!ok) {
+      set_error("prior leaf %d: bad distribution %d or parameters", i, l.dist);
+      return GL_ERR_INVALID;
+    }
+    plan->prior[i] = make_leaf(l);
+  }
+  plan->has_prior = 1;
+  return GL_OK;
+}
+
+int gl_plan_destroy(gl_plan* plan) {
+  if (!plan) return GL_OK;
+  if (plan->dev_buf) cudaFree(plan->dev_buf);
+  delete plan;
+  return GL_OK;
+}
+
+int gl_plan_query(const gl_plan* plan, int* smem_bytes, int* threads_per_block, int* max_img_pix) {
+  if (!plan) {
+    set_error("gl_plan_query: null plan");
+    return GL_ERR_INVALID;
+  }
+  if (smem_bytes) *smem_bytes = plan->smem_bytes;
+  if (threads_per_block) *threads_per_block = kThreads;
+  if (max_img_pix) *max_img_pix = plan->max_pix;
+  return GL_OK;
+}
+
+static int common_checks(const gl_plan* plan, const float* x, int bs) {
+  if (!plan || (bs > 0 && !x) || bs < 0) {
+    set_error("null plan / input or negative batch");
+    return GL_ERR_INVALID;
+  }
+  return check_device(plan);
+}
+
+int gl_forward(const gl_plan* plan, const float* x, const int* img_id, int bs, float* logL,
+               float* chi2, float* img_out, int* status, void* stream) {
+  int rc = common_checks(plan, x, bs);
+  if (rc) return rc;
+  if ((logL || chi2))
+    for (int i = 0; i < plan->n_images; ++i)
+      if (!plan->img[i].obs) {
+        set_error("image %d has no observed data; pass logL = chi2 = NULL", i);
+        return GL_ERR_INVALID;
+      }
+  FusedArgs a;
+  fill_args(plan, a);
+  a.bs = bs;
+  a.x = x;
+  a.img_id = img_id;
+  a.logL = logL;
+  a.chi2 = chi2;
+  a.img_out = img_out;
+  a.status = status;
+  return launch_fused(a, plan->smem_bytes, (cudaStream_t)stream);
+}
+
+int gl_forward_grad(const gl_plan* plan, const float* x, const int* img_id, int bs, float* logL,
+                    float* chi2, float* dlogL_dx, int* status, void* stream) {
+  int rc = common_checks(plan, x, bs);
+  if (rc) return rc;
+  for (int i = 0; i < plan->n_images; ++i)
+    if (!plan->img[i].obs) {
+      set_error("image %d has no observed data", i);
+      return GL_ERR_INVALID;
+    }
+  FusedArgs a;
+  fill_args(plan, a);
+  a.bs = bs;
+  a.x = x;
+  a.img_id = img_id;
+  a.logL = logL;
+  a.chi2 = chi2;
+  a.grad = dlogL_dx;
+  a.status = status;
+  a.want_grad = dlogL_dx != nullptr;
+  return launch_fused(a, plan->smem_bytes, (cudaStream_t)stream);
+}
+
+int gl_adjoint(const gl_plan* plan, const float* x, const int* img_id, int bs, const float* dlogL,
+               float* dx, int* status, void* stream) {
+  int rc = common_checks(plan, x, bs);
+  if (rc) return rc;
+  if (!dx || !dlogL) {
+    set_error("gl_adjoint: dlogL and dx are required");
+    return GL_ERR_INVALID;
+  }
+  FusedArgs a;
+  fill_args(plan, a);
+  a.bs = bs;
+  a.x = x;
+  a.img_id = img_id;
+  a.dlogL = dlogL;
+  a.grad = dx;
+  a.status = status;
+  a.want_grad = 1;
+  return launch_fused(a, plan->smem_bytes, (cudaStream_t)stream);
+}
+
+int gl_log_prob(const gl_plan* plan, const float* z, const int* img_id, int bs, float* logp,
+                float* chi2, float* dlogp_dz, int* status, void* stream) {
+  int rc = common_checks(plan, z, bs);
+  if (rc) return rc;
+  if (!plan->has_prior) {
+    set_error("gl_log_prob: the plan has no prior (gl_plan_set_prior)");
+    return GL_ERR_INVALID;
+  }
+  FusedArgs a;
+  fill_args(plan, a);
+  a.bs = bs;
+  a.x = z;
+  a.img_id = img_id;
+  a.logL = logp;
+  a.chi2 = chi2;
+  a.grad = dlogp_dz;
+  a.status = status;
+  a.zmode = 1;
+  a.want_grad = dlogp_dz != nullptr;
+  return launch_fused(a, plan->smem_bytes, (cudaStream_t)stream);
+}
+
+int gl_bijector_forward(const gl_plan* plan, const float* z, int bs, float* x, void* stream) {
+  int rc = common_checks(plan, z, bs);
+  if (rc) return rc;
+  if (!plan->has_prior || !x) {
+    set_error("gl_bijector_forward: plan has no prior or x is null");
+    return GL_ERR_INVALID;
+  }
+  return launch_bijector_forward(plan->prior, plan->model.n_params, z, bs, x, (cudaStream_t)stream);
+}
+
+int gl_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,
+                    const int* n_terms, float* out0, float* out1, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !y || !params || !out0))) {
+    set_error("gl_profile_eval: null pointer or negative size");
+    return GL_ERR_INVALID;
+  }
+  const bool mass = type == GL_PROF_EPL || type == GL_PROF_SHEAR || type == GL_PROF_SIS ||
+                    type == GL_PROF_SIE;
+  if (mass && !out1) {
+    set_error("gl_profile_eval: mass profiles need out1");
+    return GL_ERR_INVALID;
+  }
+  if (type == GL_PROF_EPL && !n_terms) {
+    set_error("gl_profile_eval: EPL needs the device term count");
+    return GL_ERR_INVALID;
+  }
+  return launch_profile_eval(type, x, y, n, params, n_terms, out0, out1, (cudaStream_t)stream);
+}
+
+int gl_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out,
+                      void* stream) {
+  if (n < 1 || !e1 || !e2 || !k_out || cap < 0) {
+    set_error("gl_epl_term_count: bad arguments");
+    return GL_ERR_INVALID;
+  }
+  return launch_epl_term_count(e1, e2, n, cap, k_out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

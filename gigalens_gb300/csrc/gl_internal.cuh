@@ -1,0 +1,120 @@
+// Internal structures shared by the host side of the C ABI and the kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gigalens_cuda.h"
+
+namespace gl {
+
+constexpr int kThreads = 544;        // 17 warps: 1080 conv units of a 90x90 image in 2 rounds
+constexpr int kColBlock = 8;         // output columns per thread in the PSF correlation
+constexpr int kMaxTerms = 256;       // largest EPL iteration cap the fused kernel accepts
+constexpr int kMaxKS = 25;           // largest parity sub-kernel side
+constexpr int kMaxPlanes = 4;        // supersample <= 2 in the fused kernel
+constexpr int kRedSlots = 48;        // reduced quantities per sample
+
+// Per-image constants, in device-ready form.
+struct DevImage {
+  int N;            // base pixels per side
+  int ss;           // supersampling factor
+  int nplanes;      // ss*ss parity planes of the supersampled image
+  int KS;           // parity sub-kernel side
+  int ksp;          // KS rounded up to a multiple of 4 (row pitch of a sub-kernel)
+  int d[kMaxPlanes];      // correlation offset of parity p (rows) / q (cols)
+  int pitchI;       // row pitch (floats) of an image-parity plane in shared memory
+  int padI[kMaxPlanes];   // left zero pad of plane with column parity q
+  int pitchW;       // row pitch of the likelihood-adjoint plane
+  int padW;         // its left zero pad
+  int ncb;          // column blocks of kColBlock outputs (multiple of 4)
+  int rows2;        // N rounded up to even
+  float x0, y0, t00, t01, t10, t11;   // fine grid: x = t00*col + t01*row + x0
+  float cf;         // det(transform_pix2angle), tf/simulator.py:24-26
+  float bg2;        // background_rms^2
+  float inv_t;      // 1/exp_time
+  const float* obs; // device N*N (may be null)
+  const float* grid;// device [nplanes][N][N][2]: (x, y) of each supersampled pixel, plane order
+  const float* kern;// device [nplanes][KS][ksp] forward parity sub-kernels
+  // shared-memory layout (float offsets)
+  int offI, offW, offK, smem_floats;
+};
+
+// Profile slot: columns of each canonical parameter in the flat vector.
+struct DevProfile {
+  int type;
+  int niter;
+  int col[GL_MAX_PROFILE_PARAMS];
+};
+
+struct DevPriorLeaf {
+  int dist;           // GL_DIST_*
+  float loc, scale;   // Normal / LogNormal / TruncatedNormal
+  float lo, hi;       // support of Uniform / TruncatedNormal (Sigmoid bijector range)
+  float lognorm;      // TruncatedNormal: log(Phi(beta)-Phi(alpha)); Uniform: log(high-low)
+  float loglen;       // log(high-low) of the Sigmoid bijector
+};
+
+// Model family of the fused kernel (compile-time); see gl_fused.cu.
+enum ModelFamily : int {
+  FAM_EPL_SHEAR_SE_SE = 0,  // EPL + Shear ; SersicEllipse lens light ; SersicEllipse source
+  FAM_EPL_SHEAR_SE = 1,     // EPL + Shear ; no lens light            ; SersicEllipse source
+  FAM_EPL_SE_SE = 2,        // EPL         ; SersicEllipse            ; SersicEllipse
+  FAM_EPL_SE = 3,           // EPL         ; no lens light            ; SersicEllipse
+  FAM_COUNT = 4
+};
+
+struct FusedArgs {
+  int family;
+  int d;                    // flat parameter count
+  int bs;
+  int n_images;
+  DevImage img[GL_MAX_IMAGES];
+  // slots of the compile-time family, resolved to columns
+  DevProfile epl, shear, llight, source;
+  int has_prior;
+  DevPriorLeaf prior[GL_MAX_PARAMS];
+  // inputs / outputs
+  const float* x;           // [bs,d] physical (mode x) or unconstrained z (mode z)
+  const int* img_id;        // [bs] or null
+  const float* dlogL;       // [bs] upstream weights (adjoint mode) or null
+  float* logL;              // [bs] or null
+  float* chi2;              // [bs] or null
+  float* img_out;           // [bs, maxN*maxN] or null
+  float* grad;              // [bs,d] or null
+  int* status;              // [bs] or null
+  int img_stride;           // floats per sample in img_out
+  int zmode;                // 1: x holds z; apply bijector, add prior + fldj
+  int want_grad;            // run the adjoint phases
+};
+
+}  // namespace gl
+
+struct gl_plan {
+  int device;
+  gl_model_desc model;
+  int family;
+  int n_images;
+  gl_image_desc host_img[GL_MAX_IMAGES];
+  gl::DevImage img[GL_MAX_IMAGES];
+  float* dev_buf;           // owns obs + kernels for all images
+  size_t dev_buf_bytes;
+  int smem_bytes;
+  int max_pix;              // largest N*N
+  int has_prior;
+  gl::DevPriorLeaf prior[GL_MAX_PARAMS];
+  gl::DevProfile epl, shear, llight, source;
+};
+
+namespace gl {
+// implemented in gl_fused.cu
+int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream);
+int fused_kernel_prepare(int smem_bytes);
+// implemented in gl_profile_eval.cu
+int launch_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,
+                        const int* n_terms, float* out0, float* out1, cudaStream_t stream);
+int launch_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out,
+                          cudaStream_t stream);
+int launch_bijector_forward(const DevPriorLeaf* leaves, int d, const float* z, int bs, float* x,
+                            cudaStream_t stream);
+void set_error(const char* fmt, ...);
+}  // namespace gl

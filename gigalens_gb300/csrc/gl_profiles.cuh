@@ -1,0 +1,401 @@
+// Per-pixel profile arithmetic (forward and reverse mode) shared by the fused
+// kernel and the elementwise profile kernels.
+//
+// Forward formulas follow the reference:
+//   EPL    gigalens/tf/profiles/mass/epl.py:23-68  (Tessore-Metcalf series)
+//   Shear  gigalens/tf/profiles/mass/shear.py:12-14
+//   SIS    gigalens/tf/profiles/mass/sis.py:13-18
+//   SIE    gigalens/tf/profiles/mass/sie.py:14-43
+//   Sersic gigalens/tf/profiles/light/sersic.py:25-72
+// The reverse mode is written by hand: it replaces TensorFlow autodiff and
+// differentiates the same expressions.  The EPL series is not stored: its
+// derivatives come from two extra running sums of the recomputed series,
+//   dF/da = i (2H + F),  H = sum_n n last_n     (last_n = A_n e^{i(2n+1)a})
+//   dF/df = H / f                                (A_n is proportional to f^n)
+//   dF/dt = sum_n s_n last_n, s_n = sum_{m<=n} d ln|p_m| / dt
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace gl {
+
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kLn2 = 0.6931471805599453f;
+constexpr float kHalfLog2Pi = 0.91893853320467274f;
+
+// ------------------------------------------------------------------ EPL
+struct EplC {
+  float cx, cy, cph, sph;   // centre, rotation by phi
+  float q, t, tm1, f;       // axis ratio, t = gamma-1, f = (1-q)/(1+q)
+  float A, log2b;           // A = 2b/(1+q), b = theta_E_conv*sqrt((1+q^2)/2)
+  int K;                    // series iterations
+};
+
+__device__ __forceinline__ EplC epl_consts(float theta_E, float gamma, float e1, float e2, float cx,
+                                           float cy, int K) {
+  EplC c;
+  float phi = atan2f(e2, e1) * 0.5f;
+  float cr = sqrtf(e1 * e1 + e2 * e2);
+  float cc = fminf(fmaxf(cr, 0.f), 1.f);
+  float q = (1.f - cc) / (1.f + cc);
+  float theta_E_conv = theta_E / sqrtf((1.f + q * q) / (2.f * q));
+  float b = theta_E_conv * sqrtf((1.f + q * q) / 2.f);
+  sincosf(phi, &c.sph, &c.cph);
+  c.cx = cx;
+  c.cy = cy;
+  c.q = q;
+  c.t = gamma - 1.f;
+  c.tm1 = c.t - 1.f;
+  c.f = (1.f - q) / (1.f + q);
+  c.A = (2.f * b) / (1.f + q);
+  c.log2b = log2f(b);
+  c.K = K;
+  return c;
+}
+
+// Term count rule, tf/profiles/mass/epl.py:41 and :51-56, float32 throughout.
+__device__ __forceinline__ float epl_f_of(float e1, float e2) {
+  float cc = fminf(fmaxf(sqrtf(e1 * e1 + e2 * e2), 0.f), 1.f);
+  float q = (1.f - cc) / (1.f + cc);
+  return (1.f - q) / (1.f + q);
+}
+__device__ __forceinline__ int epl_terms_from_maxf(float maxf, int cap) {
+  float niter = logf(1e-12f) / logf(maxf) + 2.f;
+  // iterations i = 1, 2, ... while i < niter, at most cap
+  int k = 0;
+  if (niter > 1.f) {                      // false for NaN
+    float c = ceilf(niter) - 1.f;
+    k = c >= (float)cap ? cap : (int)c;
+  }
+  return k;
+}
+
+// p_n = -f (2n - (2-t)) / (2n + (2-t)) with the reference's op order.
+__device__ __forceinline__ float epl_prefac(float f, float t, int n) {
+  float nn = (float)n;
+  float tt = 2.f - t;
+  return (-f * (2.f * nn - tt)) / (2.f * nn + tt);
+}
+// d ln|p_n| / dt
+__device__ __forceinline__ float epl_dlnp_dt(float t, int n) {
+  float nn = (float)n;
+  return 1.f / (2.f * nn - 2.f + t) + 1.f / (2.f * nn + 2.f - t);
+}
+
+struct EplGeom {
+  float dx, dy, xr, yr, qx, R2, invR, l2Rc, Cs, Ss, Cs2, Ss2;
+  bool clipped;
+};
+
+__device__ __forceinline__ EplGeom epl_geom(const EplC& c, float x, float y) {
+  EplGeom g;
+  g.dx = x - c.cx;
+  g.dy = y - c.cy;
+  g.xr = g.dx * c.cph + g.dy * c.sph;
+  g.yr = -g.dx * c.sph + g.dy * c.cph;
+  g.qx = c.q * g.xr;
+  g.R2 = g.qx * g.qx + g.yr * g.yr;
+  float R = sqrtf(g.R2);
+  float Rc = fminf(fmaxf(R, 1e-10f), 1e10f);
+  g.clipped = !(R >= 1e-10f && R <= 1e10f);
+  if (g.R2 > 0.f) {
+    g.invR = rsqrtf(g.R2);
+    g.Cs = g.qx * g.invR;
+    g.Ss = g.yr * g.invR;
+  } else {  // atan2(+-0, +-0): angle 0 or pi
+    g.invR = 0.f;
+    g.Cs = signbit(g.qx) ? -1.f : 1.f;
+    g.Ss = 0.f;
+  }
+  g.l2Rc = __log2f(Rc);
+  g.Cs2 = g.Cs * g.Cs - g.Ss * g.Ss;
+  g.Ss2 = 2.f * g.Cs * g.Ss;
+  return g;
+}
+
+// Forward deflection.  tab[n] = (p_n, s_n), n = 1..K.
+__device__ __forceinline__ void epl_deflect(const EplC& c, const float2* __restrict__ tab, float x,
+                                            float y, float& ax, float& ay) {
+  EplGeom g = epl_geom(c, x, y);
+  float lx = g.Cs, ly = g.Ss, Fx = g.Cs, Fy = g.Ss;
+  int n = 1;
+#pragma unroll 1
+  for (; n + 1 <= c.K; n += 2) {
+    float p0 = tab[n].x, p1 = tab[n + 1].x;
+    float u = p0 * lx, v = p0 * ly;
+    lx = fmaf(g.Cs2, u, -g.Ss2 * v);
+    ly = fmaf(g.Ss2, u, g.Cs2 * v);
+    Fx += lx;
+    Fy += ly;
+    u = p1 * lx;
+    v = p1 * ly;
+    lx = fmaf(g.Cs2, u, -g.Ss2 * v);
+    ly = fmaf(g.Ss2, u, g.Cs2 * v);
+    Fx += lx;
+    Fy += ly;
+  }
+  if (n <= c.K) {
+    float p0 = tab[n].x;
+    float u = p0 * lx, v = p0 * ly;
+    lx = fmaf(g.Cs2, u, -g.Ss2 * v);
+    ly = fmaf(g.Ss2, u, g.Cs2 * v);
+    Fx += lx;
+    Fy += ly;
+  }
+  float P = c.A * exp2f(c.tm1 * (c.log2b - g.l2Rc));
+  float arx = Fx * P, ary = Fy * P;
+  ax = arx * c.cph - ary * c.sph;
+  ay = arx * c.sph + ary * c.cph;
+}
+
+struct EplAcc {
+  float phi, SP, SPlnR, FH, FT, q, cx, cy;
+  __device__ __forceinline__ void zero() { phi = SP = SPlnR = FH = FT = q = cx = cy = 0.f; }
+};
+
+// Series state of one pixel: the deflection plus the running sums that the
+// reverse mode needs (H = sum n last_n, T = sum s_n last_n).
+struct EplState {
+  EplGeom g;
+  float Fx, Fy, Hx, Hy, Tx, Ty, P, ax, ay;
+};
+
+__device__ __forceinline__ EplState epl_state(const EplC& c, const float2* __restrict__ tab, float x,
+                                              float y) {
+  EplState s;
+  s.g = epl_geom(c, x, y);
+  float lx = s.g.Cs, ly = s.g.Ss, Fx = s.g.Cs, Fy = s.g.Ss;
+  float Hx = 0.f, Hy = 0.f, Tx = 0.f, Ty = 0.f;
+  float nf = 1.f;
+#pragma unroll 2
+  for (int n = 1; n <= c.K; ++n) {
+    float2 ps = tab[n];
+    float u = ps.x * lx, v = ps.x * ly;
+    lx = fmaf(s.g.Cs2, u, -s.g.Ss2 * v);
+    ly = fmaf(s.g.Ss2, u, s.g.Cs2 * v);
+    Fx += lx;
+    Fy += ly;
+    Hx = fmaf(nf, lx, Hx);
+    Hy = fmaf(nf, ly, Hy);
+    Tx = fmaf(ps.y, lx, Tx);
+    Ty = fmaf(ps.y, ly, Ty);
+    nf += 1.f;
+  }
+  s.Fx = Fx;
+  s.Fy = Fy;
+  s.Hx = Hx;
+  s.Hy = Hy;
+  s.Tx = Tx;
+  s.Ty = Ty;
+  s.P = c.A * exp2f(c.tm1 * (c.log2b - s.g.l2Rc));
+  float arx = Fx * s.P, ary = Fy * s.P;
+  s.ax = arx * c.cph - ary * c.sph;
+  s.ay = arx * c.sph + ary * c.cph;
+  return s;
+}
+
+// Accumulate the contribution of the deflection adjoint (abx, aby).
+__device__ __forceinline__ void epl_backprop(const EplC& c, const EplState& s, float abx, float aby,
+                                             EplAcc& acc) {
+  const EplGeom& g = s.g;
+  // rotate back by -phi
+  acc.phi += -abx * s.ay + aby * s.ax;
+  float arbx = abx * c.cph + aby * c.sph;
+  float arby = -abx * c.sph + aby * c.cph;
+  // alpha_r = P * F
+  float Pb = arbx * s.Fx + arby * s.Fy;
+  float PbP = Pb * s.P;
+  acc.SP += PbP;
+  acc.SPlnR += PbP * (kLn2 * g.l2Rc);
+  float Fbx = s.P * arbx, Fby = s.P * arby;
+  float Dx = 2.f * s.Hx + s.Fx, Dy = 2.f * s.Hy + s.Fy;
+  float ab = -Fbx * Dy + Fby * Dx;          // adjoint of the angle a
+  acc.FH += Fbx * s.Hx + Fby * s.Hy;
+  acc.FT += Fbx * s.Tx + Fby * s.Ty;
+  float Rb = g.clipped ? 0.f : -PbP * c.tm1 * g.invR;   // dP/dR = P (1-t) / R
+  float inv2 = g.invR * g.invR;
+  float qxb = Rb * g.qx * g.invR - ab * g.yr * inv2;
+  float yrb = Rb * g.yr * g.invR + ab * g.qx * inv2;
+  float xrb = qxb * c.q;
+  acc.q += qxb * g.xr;
+  float dxb = xrb * c.cph - yrb * c.sph;
+  float dyb = xrb * c.sph + yrb * c.cph;
+  acc.phi += xrb * g.yr - yrb * g.xr;
+  acc.cx -= dxb;
+  acc.cy -= dyb;
+}
+
+// Per-sample chain rule of the EPL accumulators to d/d(theta_E, gamma, e1, e2, cx, cy).
+__device__ __forceinline__ void epl_chain(float theta_E, float gamma, float e1, float e2,
+                                          const EplC& c, const EplAcc& a, float out[6]) {
+  float cr = sqrtf(e1 * e1 + e2 * e2);
+  float cc = fminf(fmaxf(cr, 0.f), 1.f);
+  float q = c.q;
+  float b = exp2f(c.log2b);
+  float lnb = kLn2 * c.log2b;
+  float tb = a.SP * lnb - a.SPlnR + a.FT;          // d/dt
+  float bb = (b != 0.f) ? a.SP * c.tm1 / b : 0.f;  // d/db via P
+  float Ab = (c.A != 0.f) ? a.SP / c.A : 0.f;       // d/dA
+  bb += Ab * 2.f / (1.f + q);
+  float qb = a.q - Ab * 2.f * b / ((1.f + q) * (1.f + q));
+  if (c.f != 0.f) qb += (a.FH / c.f) * (-2.f / ((1.f + q) * (1.f + q)));
+  // b = theta_E * sqrt(q) (the reference's two-factor form, simplified)
+  float thb = bb * sqrtf(q);
+  if (q != 0.f) qb += bb * b / (2.f * q);
+  float cb = qb * (-2.f / ((1.f + cc) * (1.f + cc)));
+  float e1b = 0.f, e2b = 0.f;
+  if (cr > 0.f && cr <= 1.f) {
+    e1b += cb * e1 / cr;
+    e2b += cb * e2 / cr;
+  }
+  float r2 = e1 * e1 + e2 * e2;
+  if (r2 > 0.f) {
+    e1b += a.phi * (-0.5f * e2 / r2);
+    e2b += a.phi * (0.5f * e1 / r2);
+  }
+  out[0] = thb;
+  out[1] = tb;
+  out[2] = e1b;
+  out[3] = e2b;
+  out[4] = a.cx;
+  out[5] = a.cy;
+}
+
+// ------------------------------------------------------------------ Sersic
+struct SerC {
+  float cx, cy, cph, sph, sq, isq;
+  float a1, a0;     // rho = (R/Rs)^(1/n) = exp2(a1*log2(R^2) - a0)
+  float nb;         // -bn*log2(e)
+  float bn, Ie;
+};
+
+__device__ __forceinline__ SerC sersic_consts(float Rs, float n, float e1, float e2, float cx,
+                                              float cy, float Ie) {
+  SerC s;
+  float phi = atan2f(e2, e1) * 0.5f;
+  float c = sqrtf(e1 * e1 + e2 * e2);
+  float q = (1.f - c) / (1.f + c);
+  sincosf(phi, &s.sph, &s.cph);
+  s.sq = sqrtf(q);
+  s.isq = 1.f / s.sq;
+  s.cx = cx;
+  s.cy = cy;
+  s.a1 = 0.5f / n;
+  s.a0 = log2f(Rs) / n;
+  s.bn = 1.9992f * n - 0.3271f;
+  s.nb = -s.bn * kLog2e;
+  s.Ie = Ie;
+  return s;
+}
+
+__device__ __forceinline__ float sersic_light(const SerC& s, float X, float Y) {
+  float dX = X - s.cx, dY = Y - s.cy;
+  float u = s.cph * dX + s.sph * dY;
+  float v = -s.sph * dX + s.cph * dY;
+  float xt1 = u * s.sq, xt2 = v * s.isq;
+  float R2 = xt1 * xt1 + xt2 * xt2;
+  float rho = exp2f(s.a1 * __log2f(R2) - s.a0);
+  return s.Ie * exp2f(s.nb * (rho - 1.f));
+}
+
+struct SerAcc {
+  float Ie, RsA, nA, bnA, sq, isq, phi, cx, cy;
+  __device__ __forceinline__ void zero() { Ie = RsA = nA = bnA = sq = isq = phi = cx = cy = 0.f; }
+};
+
+struct SerFwd {
+  float dX, dY, u, v, xt1, xt2, R2, l2, rho, E, I;
+};
+
+__device__ __forceinline__ SerFwd sersic_fwd(const SerC& s, float X, float Y) {
+  SerFwd f;
+  f.dX = X - s.cx;
+  f.dY = Y - s.cy;
+  f.u = s.cph * f.dX + s.sph * f.dY;
+  f.v = -s.sph * f.dX + s.cph * f.dY;
+  f.xt1 = f.u * s.sq;
+  f.xt2 = f.v * s.isq;
+  f.R2 = f.xt1 * f.xt1 + f.xt2 * f.xt2;
+  f.l2 = __log2f(f.R2);
+  f.rho = exp2f(s.a1 * f.l2 - s.a0);
+  f.E = exp2f(s.nb * (f.rho - 1.f));
+  f.I = s.Ie * f.E;
+  return f;
+}
+
+// Reverse of one Sersic evaluation with image adjoint Ib; returns the
+// adjoint of the evaluation coordinates in (Xb, Yb).
+__device__ __forceinline__ void sersic_reverse(const SerC& s, const SerFwd& f, float Ib,
+                                               SerAcc& a, float& Xb, float& Yb) {
+  a.Ie += Ib * f.E;
+  float rb = Ib * (-s.bn * f.I);          // adjoint of rho
+  float rr = rb * f.rho;
+  a.RsA += rr;
+  float lnrho = kLn2 * (s.a1 * f.l2 - s.a0);
+  a.nA += rr * lnrho;
+  a.bnA += Ib * f.I * (f.rho - 1.f);
+  float R2b = (f.R2 > 0.f) ? rr * s.a1 / f.R2 : 0.f;
+  float xt1b = 2.f * R2b * f.xt1, xt2b = 2.f * R2b * f.xt2;
+  float ub = xt1b * s.sq, vb = xt2b * s.isq;
+  a.sq += xt1b * f.u;
+  a.isq += xt2b * f.v;
+  float dXb = ub * s.cph - vb * s.sph;
+  float dYb = ub * s.sph + vb * s.cph;
+  a.phi += ub * f.v - vb * f.u;
+  a.cx -= dXb;
+  a.cy -= dYb;
+  Xb = dXb;
+  Yb = dYb;
+}
+
+// Per-sample chain to d/d(R_sersic, n_sersic, e1, e2, cx, cy, Ie).
+__device__ __forceinline__ void sersic_chain(float Rs, float n, float e1, float e2, const SerC& s,
+                                             const SerAcc& a, float out[7]) {
+  float c = sqrtf(e1 * e1 + e2 * e2);
+  float q = s.sq * s.sq;
+  out[0] = a.RsA * (-1.f / (n * Rs));
+  out[1] = a.nA * (-1.f / n) - a.bnA * 1.9992f;
+  float qb = a.sq * 0.5f / s.sq + a.isq * (-0.5f * s.isq / q);
+  float cb = qb * (-2.f / ((1.f + c) * (1.f + c)));
+  float e1b = 0.f, e2b = 0.f;
+  if (c > 0.f) {
+    e1b = cb * e1 / c + a.phi * (-0.5f * e2 / (c * c));
+    e2b = cb * e2 / c + a.phi * (0.5f * e1 / (c * c));
+  }
+  out[2] = e1b;
+  out[3] = e2b;
+  out[4] = a.cx;
+  out[5] = a.cy;
+  out[6] = a.Ie;
+}
+
+// ------------------------------------------------------------------ SIS / SIE
+__device__ __forceinline__ void sis_deflect(float theta_E, float cx, float cy, float x, float y,
+                                            float& ax, float& ay) {
+  float dx = x - cx, dy = y - cy;
+  float R = sqrtf(dx * dx + dy * dy);
+  float a = (R == 0.f) ? 0.f : theta_E / R;
+  ax = a * dx;
+  ay = a * dy;
+}
+
+__device__ __forceinline__ void sie_deflect(float theta_E, float e1, float e2, float cx, float cy,
+                                            float x, float y, float& ax, float& ay) {
+  float phi = atan2f(e2, e1) * 0.5f;
+  float c = fminf(sqrtf(e1 * e1 + e2 * e2), 0.9999f);
+  float q = (1.f - c) / (1.f + c);
+  float theta_E_conv = theta_E / sqrtf((1.f + q * q) / (2.f * q));
+  float b = theta_E_conv * sqrtf((1.f + q * q) / 2.f);
+  float sp, cp;
+  sincosf(phi, &sp, &cp);
+  float dx = x - cx, dy = y - cy;
+  float xr = dx * cp + dy * sp, yr = -dx * sp + dy * cp;
+  float psi = sqrtf(q * q * (xr * xr) + yr * yr);
+  float sq = sqrtf(1.f - q * q);
+  float fx = b / sq * atanf(sq * xr / psi);
+  float fy = b / sq * atanhf(sq * yr / psi);
+  ax = fx * cp - fy * sp;
+  ay = fx * sp + fy * cp;
+}
+
+}  // namespace gl

@@ -1,0 +1,208 @@
+/*
+ * gigalens_cuda.h - C ABI of libgigalens_cuda.so, the GB300 (sm_103a) device
+ * library behind the gigalens_gb300.cuda substrate.
+ *
+ * The reference (GIGA-Lens, pure Python on TensorFlow/JAX) has no FFI: its
+ * plug-in boundary is the Python class protocol of profiles, simulator and
+ * probabilistic model.  Each entry point below replaces the device work of
+ * one reference call; the replaced call is cited beside it.
+ *
+ * Conventions
+ *  - extern "C", plain pointers and sizes.  Every array argument of a compute
+ *    call is DEVICE memory of the current CUDA device unless marked "host".
+ *  - float32, row-major.  A flat parameter vector per sample holds the
+ *    physical parameters in the reference's packing order (leaves of the
+ *    parameter structure: groups lens / lens light / source, profiles in
+ *    order, keys sorted; gigalens/tf/model.py:42-49).
+ *  - Stream-ordered: compute calls enqueue on `stream` (a cudaStream_t passed
+ *    as void*, NULL = legacy default stream) and return without synchronising.
+ *  - Return 0 on success, a negative GL_ERR_* code otherwise; gl_last_error()
+ *    gives a message.  Bad values are never errors (NaN pixels are zeroed,
+ *    like gigalens/tf/simulator.py:81); bad shapes, sizes and pointers are.
+ *  - A plan is immutable after creation and may be used from several streams;
+ *    the caller owns every output buffer.
+ */
+#ifndef GIGALENS_CUDA_H
+#define GIGALENS_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GL_ABI_VERSION 1
+
+/* ---- error codes ---------------------------------------------------- */
+#define GL_OK 0
+#define GL_ERR_INVALID (-1)      /* bad argument, shape or descriptor      */
+#define GL_ERR_UNSUPPORTED (-2)  /* valid input this build does not cover   */
+#define GL_ERR_CUDA (-3)         /* a CUDA runtime call failed              */
+#define GL_ERR_NOMEM (-4)        /* device allocation failed                */
+
+/* ---- profile types (reference class names in comments) --------------- */
+#define GL_PROF_NONE 0
+#define GL_PROF_EPL 1            /* tf/profiles/mass/epl.py:9    EPL        */
+#define GL_PROF_SHEAR 2          /* tf/profiles/mass/shear.py:6  Shear      */
+#define GL_PROF_SIS 3            /* tf/profiles/mass/sis.py:9    SIS        */
+#define GL_PROF_SIE 4            /* tf/profiles/mass/sie.py:9    SIE        */
+#define GL_PROF_SERSIC 10        /* tf/profiles/light/sersic.py:9   Sersic        */
+#define GL_PROF_SERSIC_ELLIPSE 11 /* tf/profiles/light/sersic.py:62 SersicEllipse */
+#define GL_PROF_SHAPELETS 12     /* tf/profiles/light/shapelets.py:11 Shapelets */
+
+#define GL_GROUP_LENS 0
+#define GL_GROUP_LENS_LIGHT 1
+#define GL_GROUP_SOURCE 2
+
+#define GL_MAX_PROFILES 8
+#define GL_MAX_PROFILE_PARAMS 8
+#define GL_MAX_IMAGES 8
+#define GL_MAX_PARAMS 64
+
+/* Canonical parameter order per type (index into gl_profile_desc.col):
+ *   EPL:            theta_E, gamma, e1, e2, center_x, center_y
+ *   SHEAR:          gamma1, gamma2
+ *   SIS:            theta_E, center_x, center_y
+ *   SIE:            theta_E, e1, e2, center_x, center_y
+ *   SERSIC:         R_sersic, n_sersic, center_x, center_y, Ie
+ *   SERSIC_ELLIPSE: R_sersic, n_sersic, e1, e2, center_x, center_y, Ie
+ *   SHAPELETS:      beta, center_x, center_y
+ * A light profile with use_lstsq has no Ie column (col = -1).            */
+typedef struct {
+  int type;                        /* GL_PROF_*                            */
+  int group;                       /* GL_GROUP_*                           */
+  int niter;                       /* EPL: iteration cap (EPL(niter));
+                                      SHAPELETS: n_max                     */
+  int use_lstsq;                   /* light: unit amplitude, solved linearly */
+  int col[GL_MAX_PROFILE_PARAMS];  /* flat-vector column of each parameter */
+} gl_profile_desc;
+
+typedef struct {
+  int n_profiles;
+  int n_params;                    /* d, width of the flat parameter vector */
+  gl_profile_desc prof[GL_MAX_PROFILES];
+} gl_model_desc;
+
+/* One camera/data configuration (SimulatorConfig + observed data).
+ * gigalens/simulator.py:11-28, tf/simulator.py:11-56, tf/model.py:31-37.   */
+typedef struct {
+  int num_pix;                     /* N (image is N x N)                   */
+  int supersample;                 /* ss                                   */
+  float transform_pix2angle[4];    /* base-scale 2x2, row-major            */
+  int kernel_size;                 /* k, odd, of the supersampled PSF; 0 = none */
+  const float* kernel;             /* host, k*k: the supersampled PSF as the
+                                      reference's subgrid_kernel returns it
+                                      (not flipped); true convolution     */
+  const float* observed;           /* host, N*N (may be NULL for simulate-only) */
+  float background_rms;
+  float exp_time;
+} gl_image_desc;
+
+/* Prior leaf: a distribution and its default event-space bijector, one per
+ * flat-vector column (tfp JointDistribution leaves,
+ * tf/model.py:50 experimental_default_event_space_bijector).              */
+#define GL_DIST_NORMAL 1           /* Normal(a=loc, b=scale), Identity          */
+#define GL_DIST_LOGNORMAL 2        /* LogNormal(a=loc, b=scale), Exp            */
+#define GL_DIST_UNIFORM 3          /* Uniform(a=low, b=high), Sigmoid(low,high) */
+#define GL_DIST_TRUNCNORMAL 4      /* TruncatedNormal(a=loc,b=scale,c=low,d=high),
+                                      Sigmoid(low, high)                       */
+typedef struct {
+  int dist;
+  float a, b, c, d;
+} gl_prior_leaf;
+
+typedef struct gl_plan gl_plan;
+
+/* ---- library ---------------------------------------------------------- */
+int gl_abi_version(void);
+const char* gl_last_error(void);
+/* Number of SMs and the opt-in shared memory per block of the current device. */
+int gl_device_info(int* sm_count, int* smem_optin_bytes);
+
+/* ---- plans ------------------------------------------------------------ */
+/* Replaces LensSimulator.__init__ (tf/simulator.py:11-56) and the constant
+ * part of ForwardProbModel.__init__ (tf/model.py:31-37): validates the model,
+ * builds the PSF+binning sub-kernels, copies observed images to the device. */
+int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int n_images,
+                   gl_plan** out);
+/* Attach the prior (one leaf per column) for gl_log_prob / gl_log_prob_grad. */
+int gl_plan_set_prior(gl_plan* plan, const gl_prior_leaf* leaves, int n_leaves);
+int gl_plan_destroy(gl_plan* plan);
+/* Shared memory per block and threads per block the fused kernel uses. */
+int gl_plan_query(const gl_plan* plan, int* smem_bytes, int* threads_per_block, int* max_img_pix);
+
+/* ---- fused forward model + likelihood -------------------------------- */
+/* img_id: [bs] image index per sample, or NULL (all samples use image 0).
+ * status: [bs] per-sample flags (bit0 non-finite logL, bit1 non-finite
+ * gradient) or NULL.                                                      */
+
+/* LensSimulator.simulate + ForwardProbModel likelihood
+ * (tf/simulator.py:65-97, tf/model.py:76-86): x[bs,d] physical parameters ->
+ * logL[bs] (sum over pixels of the Normal log density, model-based noise),
+ * chi2[bs] (mean squared normalised residual), optional img_out[bs,N,N]
+ * (simulated image; for mixed image sizes each sample's slot is max_N^2,
+ * row-major N x N at the start).  logL/chi2 may be NULL when the image has no
+ * observed data.                                                         */
+int gl_forward(const gl_plan* plan, const float* x, const int* img_id, int bs,
+               float* logL, float* chi2, float* img_out, int* status, void* stream);
+
+/* Fused value and gradient: as gl_forward plus dlogL_dx[bs,d] = d logL / d x
+ * (hand-written adjoint of tf/model.py:76-80 through tf/simulator.py:65-97
+ * and the profiles; replaces TF GradientTape, tf/inference.py:30-33).    */
+int gl_forward_grad(const gl_plan* plan, const float* x, const int* img_id, int bs,
+                    float* logL, float* chi2, float* dlogL_dx, int* status, void* stream);
+
+/* Vector-Jacobian product: dx[b,:] = dlogL[b] * d logL_b / d x_b.          */
+int gl_adjoint(const gl_plan* plan, const float* x, const int* img_id, int bs,
+               const float* dlogL, float* dx, int* status, void* stream);
+
+/* ForwardProbModel.log_prob (tf/model.py:53-86) on unconstrained z[bs,d]:
+ * logp = logL + prior.log_prob(x) + fldj(z) with x = bijector(z); chi2 as
+ * above; dlogp_dz[bs,d] (NULL = value only).  Needs gl_plan_set_prior.    */
+int gl_log_prob(const gl_plan* plan, const float* z, const int* img_id, int bs,
+                float* logp, float* chi2, float* dlogp_dz, int* status, void* stream);
+
+/* Unconstraining bijector forward: x = bij(z) per column (tf/model.py:75).  */
+int gl_bijector_forward(const gl_plan* plan, const float* z, int bs, float* x, void* stream);
+
+/* ---- profile evaluation (the MassProfile.deriv / LightProfile.light API) */
+/* Evaluate one profile at n points.  params: [n_params_of_type, n] device
+ * (row p = canonical parameter p, one value per point).  EPL uses n_terms
+ * series iterations; gl_epl_term_count computes the reference's rule.
+ * MassProfile.deriv -> (out0, out1) = deflection; LightProfile.light -> out0.
+ * (tf/profiles/mass/*.py deriv, tf/profiles/light/sersic.py light.)        */
+int gl_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,
+                    const int* n_terms, float* out0, float* out1, void* stream);
+/* tf/profiles/mass/epl.py:41,51-56: K = min(cap, #{i=1,2,..: i < log(1e-12)/log(max f)+2})
+ * over n ellipticity pairs; writes the int K to *k_out (device).           */
+int gl_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out, void* stream);
+
+/* ---- optimizer step (graph-capturable) ------------------------------- */
+/* Keras Adam as used by ModellingSequence.MAP (tf/inference.py:34,
+ * optimizer.apply_gradients): with t = *step + 1 and lr = schedule(*step),
+ *   alpha = lr*sqrt(1-b2^t)/(1-b1^t); m += (g-m)(1-b1); v += (g^2-v)(1-b2);
+ *   var -= alpha*m/(sqrt(v)+eps),  g = grad_scale * grad,
+ * then *step += 1.  step is a device int so the call can be replayed from a
+ * CUDA graph.  Schedules: constant, or Keras PolynomialDecay
+ * lr(s) = (lr0-lr_end)(1-min(s,decay_steps)/decay_steps)^power + lr_end.  */
+#define GL_LR_CONSTANT 0
+#define GL_LR_POLYNOMIAL 1
+typedef struct {
+  int schedule;      /* GL_LR_* */
+  float lr0, lr_end, decay_steps, power;
+  float beta1, beta2, eps;
+} gl_adam_cfg;
+int gl_adam_step(float* var, float* m, float* v, const float* grad, int64_t n, float grad_scale,
+                 const gl_adam_cfg* cfg, int* step, void* stream);
+
+/* ---- diagnostics (no reference counterpart) --------------------------- */
+/* FP32 FMA throughput probe: blocks_per_sm*SMs blocks of 256 threads run
+ * 8 independent FMA chains for iters*16 steps; *flops receives the flop
+ * count of one launch (out: device scratch of >= blocks floats).  Time it
+ * with events to get the FP32 peak that the fused kernel's roofline uses. */
+int gl_probe_fp32_fma(float* out, int iters, int blocks_per_sm, double* flops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GIGALENS_CUDA_H */

@@ -1,0 +1,269 @@
+"""Parity of the fused CUDA path with the float64 oracle.
+
+Tolerances (spec bar, per quantity, against the float64 restatement):
+  images       |d| <= 1e-5 |ref| + 1e-5 max|ref|   (per pixel; the absolute
+               floor covers the faint tail, where float32 exp/pow of the
+               reference itself loses relative accuracy)
+  logL, logp   |d| <= 1e-4 |ref|  (plus 1e-3 absolute for |ref| < 10)
+  chi^2        |d| <= 1e-4 |ref|
+  gradients    |d| <= 1e-3 max(|ref|, 1e-2 rms_batch(ref))  per component
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from gigalens_gb300 import _native as N
+from gigalens_gb300 import distributions as tfd
+from gigalens_gb300.model import PhysicalModel
+from gigalens_gb300.simulator import SimulatorConfig
+from oracle import lens_oracle as O
+from tests.helpers import (ORACLE_MODEL, as_batch, default_physmodel, default_prior, demo_truth,
+                           flat_from_struct, gaussian_psf, load_golden)
+
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+
+def _setup(num_pix, ss, ksub, bs, seed=0, delta=0.065, phys=None, omodel=None, prior=None):
+    from gigalens_gb300.cuda.model import ForwardProbModel
+    from gigalens_gb300.cuda.simulator import LensSimulator
+
+    prior = prior or default_prior()
+    phys = phys or default_physmodel()
+    omodel = omodel or ORACLE_MODEL
+    cfg = SimulatorConfig(delta_pix=delta, num_pix=num_pix, supersample=ss, kernel_supersampled=ksub)
+    ocfg = O.SimConfig(delta, num_pix, ss, None if ksub is None else ksub.astype(np.float64))
+    # observed image: truth draw + noise (float64 oracle)
+    truth = prior.sample(1, seed=seed + 100)
+    im_t = O.simulate(omodel, ocfg, [[{k: v.double() for k, v in d.items()} for d in g] for g in truth])
+    rng = np.random.default_rng(seed)
+    obs = im_t[0].numpy() + rng.normal(scale=0.2, size=(num_pix, num_pix))
+    pm = ForwardProbModel(prior, obs.astype(np.float32), background_rms=0.2, exp_time=1000.0)
+    sim = LensSimulator(phys, cfg, bs=bs)
+    x_struct = prior.sample(bs, seed=seed)
+    return dict(prior=prior, cfg=cfg, ocfg=ocfg, obs=obs.astype(np.float32), pm=pm, sim=sim,
+                x_struct=x_struct, omodel=omodel)
+
+
+def _oracle_loglik(s, xflat64):
+    x = xflat64.clone().requires_grad_(True)
+    ll, chi2 = O.forward_log_likelihood_flat(s["omodel"], s["ocfg"], x, s["obs"].astype(np.float64), 0.2, 1000.0)
+    (g,) = torch.autograd.grad(ll.sum(), x)
+    return ll.detach(), chi2.detach(), g
+
+
+def _check_images(got, ref):
+    got = got.double().cpu()
+    m = ref.abs().amax(dim=(-2, -1), keepdim=True)
+    err = (got - ref).abs()
+    tol = 1e-5 * ref.abs() + 1e-5 * m
+    worst = float((err / (1e-5 * ref.abs() + 1e-5 * m)).max())
+    assert bool((err <= tol).all()), "image mismatch: worst err/tol = %.3g, max rel-to-max %.3g" % (
+        worst, float((err / m).max()))
+
+
+def _check_scalar(got, ref, rtol, atol_small=1e-3, name=""):
+    got = got.double().cpu()
+    ok = (got - ref).abs() <= rtol * ref.abs() + atol_small * (ref.abs() < 10).double()
+    assert bool(ok.all()), "%s mismatch: max rel %.3g" % (name, float(((got - ref).abs() / ref.abs()).max()))
+
+
+def _check_grad(got, ref, name="grad"):
+    got = got.double().cpu()
+    floor = 1e-2 * ref.pow(2).mean(dim=0, keepdim=True).sqrt()
+    scale = torch.maximum(ref.abs(), floor)
+    rel = (got - ref).abs() / scale
+    assert bool((rel <= 1e-3).all()), "%s mismatch: worst %.3g at %s" % (name, float(rel.max()),
+                                                                         tuple(np.unravel_index(int(rel.argmax()), rel.shape)))
+
+
+CONFIGS = {
+    # name: (num_pix, ss, supersampled kernel side, bs)
+    "config0_60px_ss2_psf21": (60, 2, 21, 13),
+    "config1_90px_ss2_psf41": (90, 2, 41, 9),
+    "ss1_psf13": (48, 1, 13, 5),
+    "ss2_nopsf": (40, 2, 0, 4),
+}
+
+
+@pytest.mark.parametrize("name", list(CONFIGS))
+def test_simulate_matches_oracle(name):
+    n, ss, k, bs = CONFIGS[name]
+    ksub = gaussian_psf(0.1, 0.065 / ss, k) if k else None
+    s = _setup(n, ss, ksub, bs)
+    img = s["sim"].simulate(s["x_struct"])
+    ref = O.simulate(ORACLE_MODEL, s["ocfg"], [[{kk: v.double() for kk, v in d.items()} for d in g]
+                                               for g in s["x_struct"]])
+    _check_images(img.reshape(ref.shape), ref)
+
+
+@pytest.mark.parametrize("name", list(CONFIGS))
+def test_loglik_chi2_grad_match_oracle(name):
+    n, ss, k, bs = CONFIGS[name]
+    ksub = gaussian_psf(0.1, 0.065 / ss, k) if k else None
+    s = _setup(n, ss, ksub, bs)
+    plan = s["sim"].prob_plan(s["pm"])
+    x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
+    logL = torch.empty(bs, device="cuda")
+    chi2 = torch.empty(bs, device="cuda")
+    grad = torch.empty_like(x)
+    N.call("gl_forward_grad", plan.handle, N.ptr(x), None, bs, N.ptr(logL), N.ptr(chi2), N.ptr(grad), None,
+           N.stream_ptr())
+    torch.cuda.synchronize()
+    ll, c2, g = _oracle_loglik(s, x.double().cpu())
+    _check_scalar(logL, ll, 1e-4, name="logL")
+    _check_scalar(chi2, c2, 1e-4, name="chi2")
+    _check_grad(grad, g)
+    # value-only path gives the same logL and chi^2
+    logL2 = torch.empty(bs, device="cuda")
+    chi22 = torch.empty(bs, device="cuda")
+    N.call("gl_forward", plan.handle, N.ptr(x), None, bs, N.ptr(logL2), N.ptr(chi22), None, None, N.stream_ptr())
+    torch.cuda.synchronize()
+    assert torch.equal(logL2, logL) and torch.equal(chi22, chi2)
+
+
+def test_log_prob_and_autograd_match_oracle():
+    """ForwardProbModel.log_prob (tf/model.py:53-86) incl. prior and bijector log-Jacobian."""
+    s = _setup(60, 2, gaussian_psf(0.1, 0.0325, 21), 11, seed=5)
+    pm, prior = s["pm"], s["prior"]
+    z = pm.bij.inverse(s["x_struct"]).float().cuda().requires_grad_(True)
+    logp, chi2 = pm.log_prob(s["sim"], z)
+    logp.sum().backward()
+    zc = z.detach().double().cpu().requires_grad_(True)
+    xs = pm.bij.forward(zc)
+    ll, ochi2 = O.forward_log_likelihood_flat(ORACLE_MODEL, s["ocfg"], flat_from_struct(xs), s["obs"].astype(np.float64),
+                                              0.2, 1000.0)
+    lp = ll + prior.log_prob(xs) + pm.unconstraining_bij.forward_log_det_jacobian(pm.pack_bij.forward(zc))
+    (gz,) = torch.autograd.grad(lp.sum(), zc)
+    _check_scalar(logp.detach(), lp.detach(), 1e-4, name="logp")
+    _check_scalar(chi2, ochi2.detach(), 1e-4, name="chi2")
+    _check_grad(z.grad, gz, "dlogp/dz")
+
+
+def test_adjoint_is_weighted_gradient():
+    s = _setup(60, 2, gaussian_psf(0.1, 0.0325, 21), 7, seed=2)
+    plan = s["sim"].prob_plan(s["pm"])
+    x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
+    bs = x.shape[0]
+    grad = torch.empty_like(x)
+    N.call("gl_forward_grad", plan.handle, N.ptr(x), None, bs, None, None, N.ptr(grad), None, N.stream_ptr())
+    w = torch.linspace(-2, 3, bs, device="cuda")
+    dx = torch.empty_like(x)
+    N.call("gl_adjoint", plan.handle, N.ptr(x), None, bs, N.ptr(w), N.ptr(dx), None, N.stream_ptr())
+    torch.cuda.synchronize()
+    assert torch.allclose(dx, grad * w[:, None], rtol=1e-6, atol=0)
+
+
+def test_round_lens_single_term():
+    """All ellipticities zero: the term-count rule gives one iteration (K = 1)."""
+    prior = default_prior()
+    s = _setup(40, 2, gaussian_psf(0.1, 0.0325, 13), 3, seed=7, prior=prior)
+    xs = s["x_struct"]
+    xs[0][0]["e1"] = torch.zeros(3)
+    xs[0][0]["e2"] = torch.zeros(3)
+    plan = s["sim"].prob_plan(s["pm"])
+    x = flat_from_struct(xs).float().cuda().contiguous()
+    logL = torch.empty(3, device="cuda")
+    N.call("gl_forward", plan.handle, N.ptr(x), None, 3, N.ptr(logL), None, None, None, N.stream_ptr())
+    torch.cuda.synchronize()
+    ll, _, _ = _oracle_loglik(s, x.double().cpu())
+    _check_scalar(logL, ll, 1e-4, name="logL")
+
+
+@pytest.mark.parametrize("variant", ["no_lens_light", "no_shear", "spherical_source"])
+def test_model_families(variant):
+    from gigalens_gb300.cuda.profiles.light import sersic
+    from gigalens_gb300.cuda.profiles.mass import epl, shear
+
+    base = default_prior()
+    lens, ll, src = base.parts
+    if variant == "no_lens_light":
+        prior = tfd.JointDistributionSequential([lens, src])
+        phys = PhysicalModel([epl.EPL(50), shear.Shear()], [], [sersic.SersicEllipse()])
+        omodel = dict(lenses=[("EPL", {"niter": 50}), ("SHEAR", {})], lens_light=[],
+                      source_light=[("SERSIC_ELLIPSE", {})])
+    elif variant == "no_shear":
+        prior = tfd.JointDistributionSequential([tfd.JointDistributionSequential([lens.parts[0]]), ll, src])
+        phys = PhysicalModel([epl.EPL(50)], [sersic.SersicEllipse()], [sersic.SersicEllipse()])
+        omodel = dict(lenses=[("EPL", {"niter": 50})], lens_light=[("SERSIC_ELLIPSE", {})],
+                      source_light=[("SERSIC_ELLIPSE", {})])
+    else:
+        sp = dict(src.parts[0].parts)
+        sp.pop("e1")
+        sp.pop("e2")
+        prior = tfd.JointDistributionSequential([lens, ll, tfd.JointDistributionSequential(
+            [tfd.JointDistributionNamed(sp)])])
+        phys = PhysicalModel([epl.EPL(50), shear.Shear()], [sersic.SersicEllipse()], [sersic.Sersic()])
+        omodel = dict(lenses=[("EPL", {"niter": 50}), ("SHEAR", {})], lens_light=[("SERSIC_ELLIPSE", {})],
+                      source_light=[("SERSIC", {})])
+    s = _setup(48, 2, gaussian_psf(0.1, 0.0325, 21), 5, seed=11, phys=phys, omodel=omodel, prior=prior)
+    plan = s["sim"].prob_plan(s["pm"])
+    x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
+    logL = torch.empty(5, device="cuda")
+    grad = torch.empty_like(x)
+    N.call("gl_forward_grad", plan.handle, N.ptr(x), None, 5, N.ptr(logL), None, N.ptr(grad), None, N.stream_ptr())
+    torch.cuda.synchronize()
+    ll, _, g = _oracle_loglik(s, x.double().cpu())
+    _check_scalar(logL, ll, 1e-4, name="logL")
+    _check_grad(grad, g)
+
+
+def test_uneven_batch_two_image_sizes():
+    """Samples of two different images (60x60 and 90x90) in one launch."""
+    from gigalens_gb300.cuda._plan import ModelLayout, Plan
+
+    prior = default_prior()
+    phys = default_physmodel()
+    lay = ModelLayout(phys)
+    imgs, obs = [], []
+    for n, k in [(60, 21), (90, 41)]:
+        cfg = SimulatorConfig(delta_pix=0.065, num_pix=n, supersample=2, kernel_supersampled=gaussian_psf(0.1, 0.0325, k))
+        o = np.random.default_rng(n).normal(scale=0.2, size=(n, n)).astype(np.float32) + 1.0
+        imgs.append(dict(sim_config=cfg, observed=o, background_rms=0.2, exp_time=1000.0))
+        obs.append(o)
+    multi = Plan(lay, imgs)
+    singles = [Plan(lay, [im]) for im in imgs]
+    bs = 9
+    x = flat_from_struct(prior.sample(bs, seed=3)).float().cuda().contiguous()
+    img_id = torch.tensor([0, 1, 1, 0, 1, 0, 0, 1, 1], dtype=torch.int32, device="cuda")
+    logL = torch.empty(bs, device="cuda")
+    grad = torch.empty_like(x)
+    N.call("gl_forward_grad", multi.handle, N.ptr(x), N.ptr(img_id), bs, N.ptr(logL), None, N.ptr(grad), None,
+           N.stream_ptr())
+    for i, p in enumerate(singles):
+        sel = (img_id == i).nonzero().flatten()
+        xs = x[sel].contiguous()
+        l1 = torch.empty(len(sel), device="cuda")
+        g1 = torch.empty_like(xs)
+        N.call("gl_forward_grad", p.handle, N.ptr(xs), None, len(sel), N.ptr(l1), None, N.ptr(g1), None,
+               N.stream_ptr())
+        torch.cuda.synchronize()
+        # the term count is per image group, so each group matches its own single-image launch
+        assert torch.allclose(logL[sel], l1, rtol=1e-6) and torch.allclose(grad[sel], g1, rtol=1e-5, atol=1e-6)
+
+
+def test_demo_fixture_on_gpu():
+    """The reference's demo observation and PSF at the notebook's truth (ss = 1)."""
+    from gigalens_gb300.cuda.model import ForwardProbModel
+    from gigalens_gb300.cuda.simulator import LensSimulator
+
+    psf = load_golden("psf.npy").astype(np.float32)
+    obs = load_golden("demo.npy").astype(np.float32)
+    ksub = psf / psf.sum()
+    cfg = SimulatorConfig(delta_pix=0.065, num_pix=60, supersample=1, kernel_supersampled=ksub)
+    prior = default_prior()
+    pm = ForwardProbModel(prior, obs, background_rms=0.2, exp_time=100.0)
+    sim = LensSimulator(default_physmodel(), cfg, bs=1)
+    truth = demo_truth()
+    z = pm.bij.inverse([[{k: torch.tensor([v], dtype=torch.float32) for k, v in d.items()} for d in g]
+                        for g in truth]).cuda()
+    logp, chi2 = pm.log_prob(sim, z)
+    ocfg = O.SimConfig(0.065, 60, 1, ksub.astype(np.float64))
+    im = O.simulate(ORACLE_MODEL, ocfg, as_batch(truth))
+    _, ochi2 = O.log_likelihood(im, obs.astype(np.float64), 0.2, 100.0)
+    assert abs(float(chi2[0]) - float(ochi2[0])) <= 1e-4 * float(ochi2[0])
+    assert 0.97 < float(chi2[0]) < 1.03

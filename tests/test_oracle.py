@@ -1,0 +1,136 @@
+"""Pins of the CPU oracle against known answers taken from the reference.
+
+The reference (TensorFlow/TFP/lenstronomy) is not importable, so the oracle is
+pinned by: the reference's own Sersic known-answer test; the reference's
+closed-form SIS and SIE deflections (which the EPL series must reproduce at
+gamma = 2); the power-law limit; the reference's demo fixture (observed image
++ PSF + the notebook's true parameters, whose chi^2 must be ~1); and float64
+finite differences for the oracle's gradients.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import lens_oracle as O
+from tests.helpers import ORACLE_MODEL, as_batch, demo_truth, load_golden
+
+D = torch.float64
+
+
+def T(v):
+    return torch.tensor(v, dtype=D)
+
+
+def _pts(n=10000, seed=0):
+    rng = np.random.default_rng(seed)
+    return torch.tensor(rng.normal(size=n)), torch.tensor(rng.normal(size=n))
+
+
+def test_sersic_half_light_kat():
+    # tests/test_profiles.py:14-26 of the reference: I(R = R_sersic, e = 0) == Ie
+    v = O.sersic_ellipse_light(T(0.0), T(1.0), T(1.0), T(2.0), T(0.0), T(0.0), T(0.0), T(0.0), T(5.0))
+    assert math.isclose(float(v), 5.0, rel_tol=1e-14)
+
+
+def test_epl_gamma2_round_equals_sis():
+    x, y = _pts()
+    k = O.epl_term_count(0.0, 0.0, 100)
+    assert k == 1
+    ax, ay = O.epl_deriv(x, y, T(1.2), T(2.0), T(0.0), T(0.0), T(0.0), T(0.0), k)
+    sx, sy = O.sis_deriv(x, y, T(1.2), T(0.0), T(0.0))
+    assert torch.allclose(ax, sx, rtol=1e-13, atol=1e-13) and torch.allclose(ay, sy, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("e1,e2", [(-0.1, 0.1), (0.1, -0.1), (0.3, 0.2), (1e-3, 1e-3)])
+def test_epl_gamma2_equals_sie(e1, e2):
+    # the reference's EPL test points (tests/test_profiles.py:50-63) against its SIE closed form
+    x, y = _pts()
+    k = O.epl_term_count(e1, e2, 1000)
+    ax, ay = O.epl_deriv(x, y, T(1.2), T(2.0), T(e1), T(e2), T(0.05), T(-0.02), k)
+    sx, sy = O.sie_deriv(x, y, T(1.2), T(e1), T(e2), T(0.05), T(-0.02))
+    assert torch.allclose(ax, sx, rtol=1e-12, atol=1e-12) and torch.allclose(ay, sy, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("gamma", [1.7, 2.2, 2.5])
+def test_epl_round_power_law(gamma):
+    x, y = _pts()
+    ax, ay = O.epl_deriv(x, y, T(1.1), T(gamma), T(0.0), T(0.0), T(0.0), T(0.0), 1)
+    R = torch.sqrt(x ** 2 + y ** 2)
+    mag = 1.1 ** (gamma - 1) * R ** (2 - gamma)
+    assert torch.allclose(ax, mag * x / R, rtol=1e-12) and torch.allclose(ay, mag * y / R, rtol=1e-12)
+
+
+def test_epl_term_count_rule():
+    # tf/profiles/mass/epl.py:41: niter = log(1e-12)/log(max f) + 2; loop while i < niter
+    assert O.epl_term_count([0.0], [0.0], 50) == 1
+    # f = 0.4 -> log(1e-12)/log(0.4) + 2 = 32.16 -> 32 iterations
+    assert O.epl_term_count([0.4], [0.0], 50) == 32
+    assert O.epl_term_count([0.4], [0.0], 20) == 20
+    assert O.epl_term_count([0.1, 0.4, -0.2], [0.0, 0.0, 0.1], 50) == 32   # batch maximum
+    assert O.epl_term_count([1.5], [0.0], 50) == 0                         # f clipped to 1
+
+
+def test_hermite_functions_orthonormal():
+    # tf/profiles/light/shapelets.py:47-48,77-85: phi_n = H_n / sqrt(2^n sqrt(pi) n!)
+    u = torch.linspace(-12, 12, 200001, dtype=D)
+    phis = O.shapelet_phi_n(u, 8)
+    w = torch.exp(-u ** 2)
+    du = float(u[1] - u[0])
+    for a in range(9):
+        for b in range(9):
+            v = float((phis[a] * phis[b] * w).sum() * du)
+            assert abs(v - (1.0 if a == b else 0.0)) < 1e-8
+
+
+def test_shapelet_order():
+    N1, N2 = O.shapelet_orders(2)
+    assert list(zip(N1, N2)) == [(0, 0), (1, 0), (0, 1), (2, 0), (1, 1), (0, 2)]
+
+
+@pytest.mark.parametrize("ss", [1, 2])
+def test_demo_fixture_chi2_at_truth(ss):
+    """The reference's demo observation at the notebook's truth: chi^2 ~ 1.
+
+    Pins grid orientation, EPL+shear, Sersic, PSF orientation, binning, the
+    conversion factor and the noise model at once (mirror-image grids give >9)."""
+    psf = load_golden("psf.npy").astype(np.float64)
+    obs = load_golden("demo.npy")
+    if ss == 1:
+        ksub = psf / psf.sum()
+    else:
+        from gigalens_gb300.simulator import supersample_kernel
+        ksub = supersample_kernel(psf, 2).astype(np.float64)
+    cfg = O.SimConfig(0.065, 60, ss, ksub)
+    im = O.simulate(ORACLE_MODEL, cfg, as_batch(demo_truth()))
+    _, chi2 = O.log_likelihood(im, obs, 0.2, 100)
+    assert 0.97 < float(chi2[0]) < 1.03
+    _, chi2_flip = O.log_likelihood(im, np.ascontiguousarray(obs[:, ::-1]), 0.2, 100)
+    assert float(chi2_flip[0]) > 5
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(3)
+    k = np.exp(-np.add.outer(np.arange(-3, 4) ** 2, np.arange(-3, 4) ** 2) / 4.0)
+    cfg = O.SimConfig(0.1, 16, 2, k / k.sum())
+    obs = rng.normal(size=(16, 16)) + 1.0
+    truth = demo_truth()
+    x0 = torch.stack([torch.as_tensor(v, dtype=D).reshape(1) for v in
+                      [truth[0][0][k] for k in sorted(truth[0][0])] +
+                      [truth[0][1][k] for k in sorted(truth[0][1])] +
+                      [truth[1][0][k] for k in sorted(truth[1][0])] +
+                      [truth[2][0][k] for k in sorted(truth[2][0])]], dim=1)
+    x0[0, 18] = 0.05   # source e1 away from 0 (sqrt gradient)
+    x0[0, 19] = -0.04
+    x = x0.clone().requires_grad_(True)
+    ll, _ = O.forward_log_likelihood_flat(ORACLE_MODEL, cfg, x, obs, 0.2, 100.0)
+    (g,) = torch.autograd.grad(ll.sum(), x)
+    h = 1e-6
+    for j in range(x0.shape[1]):
+        e = torch.zeros_like(x0)
+        e[0, j] = h
+        lp, _ = O.forward_log_likelihood_flat(ORACLE_MODEL, cfg, x0 + e, obs, 0.2, 100.0)
+        lm, _ = O.forward_log_likelihood_flat(ORACLE_MODEL, cfg, x0 - e, obs, 0.2, 100.0)
+        fd = float((lp - lm) / (2 * h))
+        assert abs(fd - float(g[0, j])) <= 1e-5 * max(1.0, abs(fd)), (j, fd, float(g[0, j]))
