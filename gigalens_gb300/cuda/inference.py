@@ -1,17 +1,38 @@
 """``ModellingSequence`` of the CUDA substrate (``gigalens/tf/inference.py``).
 
-MAP: multi-start Adam on the unconstrained parameters of ``n_samples``
-chains (``tf/inference.py:17-41``).  One iteration is two device launches --
-the fused log-posterior+gradient kernel and the Adam kernel -- captured once
-in a CUDA graph and replayed ``num_steps`` times; chi^2 of every chain stays
-on the device (the reference synchronises every step for its progress bar,
-``tf/inference.py:40``; here the per-step minimum is recorded on the device in
-``map_chi2_history``).
+MAP (``tf/inference.py:17-41``): multi-start Adam on the unconstrained
+parameters of ``n_samples`` chains.  One iteration is two launches of this
+library -- the fused log-posterior+gradient kernel and the Adam kernel --
+captured once in a CUDA graph and replayed; chi^2 stays on the device (the
+reference synchronises every step for its progress bar, ``:40``; here the
+per-step minimum is recorded on the device in ``map_chi2_history``).
+
+SVI (``tf/inference.py:43-73``): full-covariance Gaussian guide
+``MultivariateNormalTriL(loc, FillScaleTriL(Exp diag, shift 1e-6))``, the
+reparameterised reverse-KL loss of ``tfp.vi.fit_surrogate_posterior``
+(mean over ``n_vi`` draws of log q(z) - log p(z)), Adam on (loc, raw scale);
+the whole step (draws, fused kernel, autograd of the guide, Adam) is one
+CUDA graph.
+
+HMC (``tf/inference.py:75-141``): preconditioned HMC with momentum
+p ~ N(0, Sigma_q^-1) (precision = the SVI covariance, as
+``MultivariateNormalPrecisionFactorLinearOperator(chol(Sigma), Sigma)``),
+leapfrog, Metropolis correction per chain, dual-averaging step-size
+adaptation (Hoffman & Gelman 2014 as in TFP's
+``DualAveragingStepSizeAdaptation``: target 0.75, shrinkage 0.05, t0 10,
+kappa 0.75, log-harmonic-mean-exp over chains) and, optionally, ChEES
+trajectory-length adaptation (Hoffman, Radul & Sountsov 2021) over the first
+80 % of the burn-in.  With a fixed trajectory (``adapt_trajectory=False``)
+one full HMC iteration (L leapfrog steps) is one CUDA graph.  TFP's random
+streams are not reproduced; the samplers are checked statistically.
 """
+import math
+
+import numpy as np
 import torch
 
 from .. import inference as _inf
-from .model import log_prob_and_grad
+from .model import _LogProb, log_prob_and_grad
 from .optimizers import Adam, AdamState
 from .simulator import LensSimulator
 
@@ -69,9 +90,274 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
         self.map_log_prob = logp
         return trial
 
-    def SVI(self, optimizer, start, n_vi=250, init_scales=1e-3, num_steps=500, seed=2):
-        raise NotImplementedError
+    # ------------------------------------------------------------------ SVI
+    def SVI(self, optimizer, start, n_vi=250, init_scales=1e-3, num_steps=500, seed=2, use_graph=True):
+        """Returns ``(q_z, losses)`` like the reference (unconstrained space)."""
+        dev = _cuda_dev()
+        start = torch.as_tensor(start, dtype=torch.float32).reshape(-1).to(dev)
+        d = start.numel()
+        scale = torch.as_tensor(np.ones(d, np.float32) * init_scales if np.size(init_scales) == 1
+                                else np.asarray(init_scales, np.float32), device=dev)
+        ntril = d * (d - 1) // 2
+        theta = torch.zeros(2 * d + ntril, dtype=torch.float32, device=dev)
+        theta[:d] = start
+        theta[d:2 * d] = torch.log(scale - 1e-6)        # FillScaleTriL: diag = exp(raw) + 1e-6
+        theta.requires_grad_(True)
+        rows, cols = torch.tril_indices(d, d, -1, device=dev)
+        diag_idx = torch.arange(d, device=dev)
+        lens_sim = LensSimulator(self.phys_model, self.sim_config, bs=n_vi)
+        plan = lens_sim.prob_plan(self.prob_model)
+        state = AdamState(theta, optimizer if optimizer is not None else Adam(1e-3))
+        losses = torch.zeros(max(num_steps, 1), dtype=torch.float32, device=dev)
+        log2pi = math.log(2 * math.pi)
+        torch.cuda.manual_seed(seed)
+        grad_buf = torch.zeros_like(theta)
 
+        def scale_tril(th):
+            L = torch.zeros(d, d, dtype=th.dtype, device=dev)
+            L = L.index_put((rows, cols), th[2 * d:])
+            return L.index_put((diag_idx, diag_idx), torch.exp(th[d:2 * d]) + 1e-6)
+
+        def step():
+            eps = torch.randn(n_vi, d, device=dev)
+            L = scale_tril(theta)
+            z = theta[:d] + eps @ L.T
+            logp, _ = _LogProb.apply(z, plan, None)
+            logq = -0.5 * (eps * eps).sum(1) - torch.log(torch.diagonal(L)).sum() - 0.5 * d * log2pi
+            loss = (logq - logp).mean()
+            (g,) = torch.autograd.grad(loss, theta)
+            grad_buf.copy_(g)
+            losses.index_copy_(0, state.step.long().clamp_(max=losses.numel() - 1), loss.detach().reshape(1))
+            state.apply(grad_buf)
+
+        if num_steps > 0:
+            _run_steps(step, num_steps, use_graph)
+        with torch.no_grad():
+            q_z = MultivariateNormalTriL(theta.detach()[:d].clone(), scale_tril(theta.detach()).clone())
+        return q_z, losses[:num_steps]
+
+    # ------------------------------------------------------------------ HMC
     def HMC(self, q_z, init_eps=0.3, init_l=3, n_hmc=50, num_burnin_steps=250, num_results=750,
-            max_leapfrog_steps=30, seed=3):
-        raise NotImplementedError
+            max_leapfrog_steps=30, seed=3, adapt_trajectory=True, adapt_step_size=True,
+            target_accept_prob=0.75, use_graph=True):
+        """Returns ``(samples, sample_stats)``; samples ``(num_results, n_hmc, d)``
+        in unconstrained space."""
+        dev = _cuda_dev()
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(seed)
+        lens_sim = LensSimulator(self.phys_model, self.sim_config, bs=n_hmc)
+        plan = lens_sim.prob_plan(self.prob_model)
+        cov = q_z.covariance().to(dev, torch.float32)
+        Lq = torch.linalg.cholesky(cov.double()).float()
+        d = cov.shape[0]
+        z = q_z.sample(n_hmc, generator=gen).to(dev).contiguous()
+        torch.cuda.manual_seed(seed)   # leapfrog draws use the default generator (graph-capturable)
+        logp = torch.empty(n_hmc, device=dev)
+        chi2 = torch.empty(n_hmc, device=dev)
+        g = torch.empty_like(z)
+        log_prob_and_grad(plan, z, logp, chi2, g)
+        n_adapt = int(num_burnin_steps * 0.8)
+        da = _DualAveraging(init_eps, target_accept_prob, dev)
+        chees = _ChEES(init_l * init_eps, max_leapfrog_steps, dev) if adapt_trajectory else None
+        total = num_burnin_steps + num_results
+        samples = torch.empty((num_results, n_hmc, d), dtype=torch.float32, device=dev)
+        acc_trace = torch.empty(total, dtype=torch.float32, device=dev)
+        eps_trace = torch.empty(total, dtype=torch.float32, device=dev)
+        L_trace = []
+        # buffers reused by every iteration (graph-stable)
+        zp, gp, lpp = torch.empty_like(z), torch.empty_like(g), torch.empty_like(logp)
+        p0 = torch.empty_like(z)
+        pp = torch.empty_like(z)
+        u_acc = torch.empty(n_hmc, device=dev)
+        eps_dev = da.step_size                  # (1,) device tensor
+
+        def kinetic(p):
+            q = p @ Lq                          # K = 0.5 p^T Sigma p = 0.5 |Lq^T p|^2
+            return 0.5 * (q * q).sum(1)
+
+        def leapfrog(L):
+            xi = torch.randn(n_hmc, d, device=dev)
+            p0.copy_(torch.linalg.solve_triangular(Lq.T, xi.T, upper=True).T)   # p ~ N(0, Sigma^-1)
+            zp.copy_(z)
+            gp.copy_(g)
+            pp.copy_(p0 + 0.5 * eps_dev * gp)
+            for i in range(L):
+                zp.add_(eps_dev * (pp @ cov))
+                log_prob_and_grad(plan, zp, lpp, chi2, gp)
+                pp.add_((eps_dev if i < L - 1 else 0.5 * eps_dev) * gp)
+            log_accept = (lpp - kinetic(pp)) - (logp - kinetic(p0))
+            log_accept = torch.nan_to_num(log_accept, nan=-float("inf"))
+            u_acc.copy_(torch.rand(n_hmc, device=dev))
+            accept = torch.log(u_acc) < log_accept
+            z.copy_(torch.where(accept[:, None], zp, z))
+            g.copy_(torch.where(accept[:, None], gp, g))
+            logp.copy_(torch.where(accept, lpp, logp))
+            return log_accept
+
+        graphs = {}
+        for it in range(total):
+            adapting = it < n_adapt
+            if chees is not None and adapting:
+                L = chees.draw_steps(float(eps_dev), gen)
+            elif chees is not None:
+                L = chees.final_steps(float(eps_dev))
+            else:
+                L = int(init_l)
+            L_trace.append(L)
+            z_before = z.clone() if (chees is not None and adapting) else None
+            if use_graph and not (chees is not None and adapting):
+                gph = graphs.get(L)
+                if gph is None:
+                    gph = _capture(lambda: leapfrog(L))
+                    graphs[L] = gph
+                gph.graph.replay()
+                log_accept = gph.out
+            else:
+                log_accept = leapfrog(L)
+            acc = torch.exp(torch.clamp(log_accept, max=0.0)).mean()
+            acc_trace[it] = acc
+            if adapt_step_size and adapting:
+                da.update(log_accept)
+            elif adapt_step_size and it == n_adapt:
+                da.finalize()
+            if z_before is not None:
+                chees.update(z_before, z, pp @ cov, log_accept, L, float(eps_dev))
+            eps_trace[it] = eps_dev[0]
+            if it >= num_burnin_steps:
+                samples[it - num_burnin_steps].copy_(z)
+        stats = {"accept_ratio": acc_trace, "step_size": eps_trace,
+                 "leapfrog_steps": torch.tensor(L_trace), "target_log_prob": logp}
+        return samples, stats
+
+
+class _Captured:
+    def __init__(self, graph, out):
+        self.graph = graph
+        self.out = out
+
+
+def _capture(fn):
+    """Warm up ``fn`` once on a side stream, then capture it in a CUDA graph."""
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        fn()
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out = fn()
+    return _Captured(g, out)
+
+
+def _run_steps(step, num_steps, use_graph):
+    """Run ``step`` ``num_steps`` times: eagerly once, then from a CUDA graph."""
+    step()
+    if num_steps == 1:
+        return
+    if not use_graph:
+        for _ in range(num_steps - 1):
+            step()
+        return
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            step()
+    torch.cuda.current_stream().wait_stream(s)
+    for _ in range(num_steps - 1):
+        g.replay()
+
+
+class MultivariateNormalTriL:
+    """The SVI guide: N(loc, L L^T) in unconstrained space."""
+
+    def __init__(self, loc, scale_tril):
+        self.loc = loc
+        self.scale_tril = scale_tril
+
+    def mean(self):
+        return self.loc
+
+    def covariance(self):
+        return self.scale_tril @ self.scale_tril.T
+
+    def sample(self, n=(), seed=None, generator=None):
+        shape = (n,) if isinstance(n, int) else tuple(n)
+        if generator is None:
+            generator = torch.Generator(device=self.loc.device)
+            generator.manual_seed(0 if seed is None else int(seed))
+        eps = torch.randn(*shape, self.loc.numel(), device=self.loc.device, generator=generator)
+        return self.loc + eps @ self.scale_tril.T
+
+    def log_prob(self, z):
+        r = torch.linalg.solve_triangular(self.scale_tril, (z - self.loc).reshape(-1, self.loc.numel()).T,
+                                          upper=False).T
+        d = self.loc.numel()
+        return (-0.5 * (r * r).sum(1) - torch.log(torch.diagonal(self.scale_tril)).sum()
+                - 0.5 * d * math.log(2 * math.pi))
+
+
+class _DualAveraging:
+    """Shared step size adapted toward ``target`` mean acceptance."""
+
+    def __init__(self, init_eps, target, dev, shrinkage=0.05, t0=10.0, kappa=0.75):
+        self.step_size = torch.tensor([float(init_eps)], device=dev)
+        self.mu = math.log(10.0 * init_eps)
+        self.target, self.gamma, self.t0, self.kappa = target, shrinkage, t0, kappa
+        self.err_sum = torch.zeros(1, device=dev)
+        self.log_avg = torch.tensor([math.log(init_eps)], device=dev)
+        self.t = 0
+
+    def update(self, log_accept):
+        self.t += 1
+        t = float(self.t)
+        # log-harmonic-mean-exp of the acceptance ratios over chains
+        la = torch.clamp(log_accept, max=0.0)
+        red = -(torch.logsumexp(-la, 0) - math.log(la.numel()))
+        p = torch.exp(red)
+        self.err_sum += self.target - p
+        log_eps = self.mu - math.sqrt(t) / self.gamma * self.err_sum / (t + self.t0)
+        w = t ** (-self.kappa)
+        self.log_avg = w * log_eps + (1 - w) * self.log_avg
+        self.step_size.copy_(torch.exp(log_eps))
+
+    def finalize(self):
+        self.step_size.copy_(torch.exp(self.log_avg))
+
+
+class _ChEES:
+    """Trajectory length adaptation by the ChEES criterion (jittered lengths,
+    Adam on log T with learning rate 0.025, beta1 = 0)."""
+
+    def __init__(self, init_T, max_steps, dev, lr=0.025, beta2=0.95):
+        self.logT = math.log(max(init_T, 1e-6))
+        self.max_steps = int(max_steps)
+        self.lr, self.b2, self.v, self.k = lr, beta2, 0.0, 0
+        self.avg_logT = self.logT
+        self.u = 1.0
+
+    def draw_steps(self, eps, gen):
+        self.u = float(torch.rand(1, generator=gen, device=gen.device)) * 0.999 + 0.001
+        T = math.exp(self.logT) * self.u
+        return int(min(self.max_steps, max(1, math.ceil(T / max(eps, 1e-12)))))
+
+    def final_steps(self, eps):
+        return int(min(self.max_steps, max(1, math.ceil(math.exp(self.avg_logT) / max(eps, 1e-12)))))
+
+    def update(self, z0, z1, v1, log_accept, L, eps):
+        a = torch.exp(torch.clamp(log_accept, max=0.0))
+        m0 = z0.mean(0, keepdim=True)
+        m1 = z1.mean(0, keepdim=True)
+        diff = ((z1 - m1) ** 2).sum(1) - ((z0 - m0) ** 2).sum(1)
+        gT = float((a * diff * ((z1 - m1) * v1).sum(1)).sum() / a.sum().clamp_min(1e-12)) * self.u
+        g = -gT * math.exp(self.logT)          # gradient of -ChEES with respect to log T
+        if not math.isfinite(g):
+            return
+        self.k += 1
+        self.v = self.b2 * self.v + (1 - self.b2) * g * g
+        vhat = self.v / (1 - self.b2 ** self.k)
+        self.logT -= self.lr * g / (math.sqrt(vhat) + 1e-8)
+        self.logT = min(self.logT, math.log(self.max_steps * max(eps, 1e-12)))
+        w = self.k ** -0.75
+        self.avg_logT = w * self.logT + (1 - w) * self.avg_logT
