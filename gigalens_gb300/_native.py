@@ -89,6 +89,7 @@ class gl_image_desc(ctypes.Structure):
         ("observed", ctypes.POINTER(ctypes.c_float)),
         ("background_rms", ctypes.c_float),
         ("exp_time", ctypes.c_float),
+        ("err_map", ctypes.POINTER(ctypes.c_float)),
     ]
 
 
@@ -142,6 +143,9 @@ SIGNATURES = [
     ("gl_epl_term_count", _i, [_vp, _vp, _i64, _i, _vp, _vp]),
     ("gl_adam_step", _i, [_vp, _vp, _vp, _vp, _i64, ctypes.c_float, ctypes.POINTER(gl_adam_cfg), _vp, _vp]),
     ("gl_probe_fp32_fma", _i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_double), _vp]),
+    ("gl_shapelets_eval", _i, [_i, _vp, _vp, _i64, _vp, _vp, _vp, _vp]),
+    ("gl_lstsq_workspace", _i, [_vp, _i, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_i)]),
+    ("gl_lstsq", _i, [_vp, _vp, _vp, _i, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp]),
 ]
 
 _lock = threading.Lock()

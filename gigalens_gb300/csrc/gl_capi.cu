@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "gl_internal.cuh"
+#include "gl_lstsq.cuh"
 
 namespace gl {
 
@@ -110,7 +111,7 @@ static int resolve_family(const gl_model_desc* m, int* family, DevProfile* epl, 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 struct HostImage {
-  std::vector<float> obs, grid, kern;
+  std::vector<float> obs, grid, kern, err;
 };
 
 // Fill the device-ready description of one image; host arrays go to hi.
@@ -226,6 +227,16 @@ static int build_image(const gl_image_desc& g, DevImage& I, HostImage& hi) {
   I.bg2 = g.background_rms * g.background_rms;
   I.inv_t = 1.f / g.exp_time;
   if (g.observed) hi.obs.assign(g.observed, g.observed + (size_t)N * N);
+  // noise map of the least-squares path: given, or the BackwardProbModel
+  // data-based map sqrt(bg^2 + clip(obs, 0, inf) / t) in float32
+  if (g.err_map) {
+    hi.err.assign(g.err_map, g.err_map + (size_t)N * N);
+  } else if (g.observed) {
+    hi.err.resize((size_t)N * N);
+    const float bg2 = g.background_rms * g.background_rms;
+    for (size_t p = 0; p < hi.err.size(); ++p)
+      hi.err[p] = sqrtf(bg2 + fmaxf(g.observed[p], 0.f) / g.exp_time);
+  }
   return GL_OK;
 }
 
@@ -337,8 +348,18 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
   memset(plan, 0, sizeof(*plan));
   plan->model = *model;
   plan->n_images = n_images;
-  int rc = resolve_family(model, &plan->family, &plan->epl, &plan->shear, &plan->llight,
-                          &plan->source);
+  // a model whose light is solved linearly runs on the least-squares kernels
+  bool lsq_model = false;
+  for (int i = 0; i < model->n_profiles; ++i)
+    if (model->prof[i].group != GL_GROUP_LENS &&
+        (model->prof[i].use_lstsq || model->prof[i].type == GL_PROF_SHAPELETS))
+      lsq_model = true;
+  int rc = GL_OK;
+  if (lsq_model) {
+    plan->family = -1;
+  } else {
+    rc = resolve_family(model, &plan->family, &plan->epl, &plan->shear, &plan->llight, &plan->source);
+  }
   if (rc) {
     delete plan;
     return rc;
@@ -368,7 +389,7 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
   plan->smem_bytes = smem_floats * 4;
   const int static_smem = 8 * 1024;   // SmemStatic upper bound
-  if (plan->smem_bytes + static_smem > dev_smem) {
+  if (!lsq_model && plan->smem_bytes + static_smem > dev_smem) {
     set_error("image needs %d bytes of shared memory; the device allows %d per block",
               plan->smem_bytes + static_smem, dev_smem);
     delete plan;
@@ -395,7 +416,12 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
     I.kern = put(hi[i].kern);
   }
   rc = cuda_check(cudaGetLastError(), "plan upload");
-  if (!rc) rc = fused_kernel_prepare(plan->smem_bytes);
+  if (!rc && !lsq_model) rc = fused_kernel_prepare(plan->smem_bytes);
+  if (!rc && lsq_model) {
+    std::vector<std::vector<float>> errs(n_images);
+    for (int i = 0; i < n_images; ++i) errs[i] = hi[i].err;
+    rc = lsq_prepare(plan, errs);
+  }
   if (rc) {
     cudaFree(plan->dev_buf);
     delete plan;
@@ -428,9 +454,47 @@ int gl_plan_set_prior(gl_plan* plan, const gl_prior_leaf* leaves, int n_leaves) 
 
 int gl_plan_destroy(gl_plan* plan) {
   if (!plan) return GL_OK;
+  lsq_destroy(plan);
   if (plan->dev_buf) cudaFree(plan->dev_buf);
   delete plan;
   return GL_OK;
+}
+
+int gl_lstsq_workspace(const gl_plan* plan, int bs, size_t* bytes, int* n_channels) {
+  if (!plan || bs < 0 || !bytes) {
+    set_error("gl_lstsq_workspace: bad arguments");
+    return GL_ERR_INVALID;
+  }
+  if (!plan->lsq) {
+    set_error("the plan has no linear-amplitude light profiles");
+    return GL_ERR_INVALID;
+  }
+  *bytes = lsq_workspace_bytes((const LsqPlan*)plan->lsq, bs);
+  if (n_channels) *n_channels = ((const LsqPlan*)plan->lsq)->D;
+  return GL_OK;
+}
+
+int gl_lstsq(const gl_plan* plan, const float* x, const int* img_id, int bs, void* work,
+             size_t work_bytes, float* coeffs, float* img_out, float* logL, float* chi2,
+             void* stream) {
+  if (!plan || (bs > 0 && (!x || !work || !coeffs)) || bs < 0) {
+    set_error("gl_lstsq: null plan, input, workspace or coeffs");
+    return GL_ERR_INVALID;
+  }
+  if (!plan->lsq) {
+    set_error("the plan has no linear-amplitude light profiles");
+    return GL_ERR_INVALID;
+  }
+  int rc = check_device(plan);
+  if (rc) return rc;
+  if (logL || chi2)
+    for (int i = 0; i < plan->n_images; ++i)
+      if (!plan->img[i].obs) {
+        set_error("image %d has no observed data", i);
+        return GL_ERR_INVALID;
+      }
+  return lsq_run(plan, x, img_id, bs, (float*)work, work_bytes, coeffs, img_out, logL, chi2,
+                 (cudaStream_t)stream);
 }
 
 int gl_plan_query(const gl_plan* plan, int* smem_bytes, int* threads_per_block, int* max_img_pix) {
@@ -448,6 +512,10 @@ static int common_checks(const gl_plan* plan, const float* x, int bs) {
   if (!plan || (bs > 0 && !x) || bs < 0) {
     set_error("null plan / input or negative batch");
     return GL_ERR_INVALID;
+  }
+  if (plan->family < 0) {
+    set_error("the plan's light profiles are solved linearly: use gl_lstsq");
+    return GL_ERR_UNSUPPORTED;
   }
   return check_device(plan);
 }
@@ -565,6 +633,15 @@ int gl_profile_eval(int type, const float* x, const float* y, int64_t n, const f
     return GL_ERR_INVALID;
   }
   return launch_profile_eval(type, x, y, n, params, n_terms, out0, out1, (cudaStream_t)stream);
+}
+
+int gl_shapelets_eval(int n_max, const float* x, const float* y, int64_t n, const float* params,
+                      const float* amps, float* out, void* stream) {
+  if (n_max < 0 || n_max > 30 || n < 0 || (n > 0 && (!x || !y || !params || !out))) {
+    set_error("gl_shapelets_eval: bad arguments");
+    return GL_ERR_INVALID;
+  }
+  return launch_shapelets_eval(n_max, x, y, n, params, amps, out, (cudaStream_t)stream);
 }
 
 int gl_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out,

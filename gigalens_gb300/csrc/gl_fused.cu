@@ -21,6 +21,7 @@
 #include <cstdio>
 
 #include "gl_internal.cuh"
+#include "gl_corr.cuh"
 #include "gl_profiles.cuh"
 
 namespace gl {
@@ -156,39 +157,6 @@ __device__ __forceinline__ void block_reduce(float (&v)[NV], SmemStatic& s) {
   __syncthreads();
 }
 
-// ---------------------------------------------------------------- correlation
-// acc[c] += sum_l k[l] * seg[c + l]  (REV: k[KS-1-l]); seg and krow 16-byte aligned.
-template <int KS, bool REV>
-__device__ __forceinline__ void corr_row(const float* __restrict__ seg,
-                                         const float* __restrict__ krow, float (&acc)[kColBlock]) {
-  constexpr int SEGN = (kColBlock + KS - 1 + 3) & ~3;
-  constexpr int KSP = (KS + 3) & ~3;
-  float s[SEGN];
-  float k[KSP];
-#pragma unroll
-  for (int i = 0; i < SEGN / 4; ++i) {
-    float4 t = reinterpret_cast<const float4*>(seg)[i];
-    s[4 * i] = t.x;
-    s[4 * i + 1] = t.y;
-    s[4 * i + 2] = t.z;
-    s[4 * i + 3] = t.w;
-  }
-#pragma unroll
-  for (int i = 0; i < KSP / 4; ++i) {
-    float4 t = reinterpret_cast<const float4*>(krow)[i];
-    k[4 * i] = t.x;
-    k[4 * i + 1] = t.y;
-    k[4 * i + 2] = t.z;
-    k[4 * i + 3] = t.w;
-  }
-#pragma unroll
-  for (int l = 0; l < KS; ++l) {
-    const float kv = REV ? k[KS - 1 - l] : k[l];
-#pragma unroll
-    for (int c = 0; c < kColBlock; ++c) acc[c] = fmaf(kv, s[c + l], acc[c]);
-  }
-}
-
 // Conv unit u -> (row i, first column j0).  Eight consecutive units form two
 // rows x four column blocks, which keeps 16-byte shared loads conflict-free
 // when the plane pitch is an odd multiple of four floats.
@@ -274,24 +242,6 @@ __device__ void phase_conv_adjoint(const DevImage& I, float* sm) {
       if (j0 + c < I.N) dst[c] = acc[c];
   }
 }
-
-#define GL_KS_DISPATCH(KSVAL, CALL) \
-  switch (KSVAL) {                  \
-    case 1: CALL(1); break;         \
-    case 3: CALL(3); break;         \
-    case 5: CALL(5); break;         \
-    case 7: CALL(7); break;         \
-    case 9: CALL(9); break;         \
-    case 11: CALL(11); break;       \
-    case 13: CALL(13); break;       \
-    case 15: CALL(15); break;       \
-    case 17: CALL(17); break;       \
-    case 19: CALL(19); break;       \
-    case 21: CALL(21); break;       \
-    case 23: CALL(23); break;       \
-    case 25: CALL(25); break;       \
-    default: break;                 \
-  }
 
 // ---------------------------------------------------------------- per-sample consts
 template <int FAM>

@@ -103,6 +103,7 @@ struct gl_plan {
   int has_prior;
   gl::DevPriorLeaf prior[GL_MAX_PARAMS];
   gl::DevProfile epl, shear, llight, source;
+  void* lsq;                // gl::LsqPlan of the least-squares path, or null
 };
 
 namespace gl {
@@ -112,6 +113,8 @@ int fused_kernel_prepare(int smem_bytes);
 // implemented in gl_profile_eval.cu
 int launch_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,
                         const int* n_terms, float* out0, float* out1, cudaStream_t stream);
+int launch_shapelets_eval(int n_max, const float* x, const float* y, int64_t n, const float* params,
+                          const float* amps, float* out, cudaStream_t stream);
 int launch_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out,
                           cudaStream_t stream);
 int launch_bijector_forward(const DevPriorLeaf* leaves, int d, const float* z, int bs, float* x,

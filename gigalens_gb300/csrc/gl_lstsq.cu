@@ -1,0 +1,754 @@
+// Linear-amplitude path: LensSimulator.lstsq_simulate (tf/simulator.py:99-165).
+//
+//   basis kernel   per (sample, band of output rows): ray-trace the band's
+//                  supersampled pixels once (beta kept in shared memory), then
+//                  for every basis channel (unit-amplitude lens-light Sersic,
+//                  shapelet (n1, n2) functions of the source) evaluate the
+//                  channel on the band, apply PSF + binning with the same
+//                  parity-plane correlation as the fused kernel, and store the
+//                  binned basis X[b][c][pixel] (unweighted, as `ret`)
+//   gram kernel    G_b = X^T W^2 X and h_b = X^T W^2 y, W = 1/err_map
+//   solve kernel   coeffs = pinv(G, rcond=1e-6) h: cyclic Jacobi
+//                  eigen-decomposition of the symmetric G (for a symmetric
+//                  matrix the singular values are |eigenvalues|), eigenvalues
+//                  with |lambda| <= rcond * max|lambda| dropped, as
+//                  tf.linalg.pinv does
+//   image kernel   img = sum_c coeffs_c X_c (no conversion factor, as the
+//                  reference), Gaussian log-likelihood with the data-based
+//                  error map and chi^2 (BackwardProbModel, tf/model.py:157-163)
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gl_corr.cuh"
+#include "gl_internal.cuh"
+#include "gl_profiles.cuh"
+#include "gl_lstsq.cuh"
+
+namespace gl {
+
+// ------------------------------------------------------------------ device helpers
+__device__ __forceinline__ float lpget(const float* sx, int col, float dflt) {
+  return col >= 0 ? sx[col] : dflt;
+}
+
+// Normalised Hermite function value phi_n(u) without the Gaussian:
+// H_n(u) / sqrt(2^n sqrt(pi) n!), recursion H_n = 2 (u H_{n-1} - (n-1) H_{n-2})
+// (tf/profiles/light/shapelets.py:47-48,77-85).
+__device__ __forceinline__ float hermite_fn(int n, float u, const float* pref) {
+  float h0 = 1.f, h1 = 2.f * u;
+  if (n == 0) return h0 * pref[0];
+  for (int i = 2; i <= n; ++i) {
+    const float h2 = 2.f * (u * h1 - (float)(i - 1) * h0);
+    h0 = h1;
+    h1 = h2;
+  }
+  return h1 * pref[n];
+}
+
+struct LsqShared {
+  float x[GL_MAX_PARAMS];
+  float2 tab[kMaxTerms + 2];
+  float red[kThreads / 32][4];
+  int K[GL_MAX_IMAGES];
+};
+
+__device__ void lsq_term_counts(const LsqArgs& a, LsqShared& st) {
+  float mx[GL_MAX_IMAGES];
+  for (int i = 0; i < GL_MAX_IMAGES; ++i) mx[i] = 0.f;
+  const int c1 = a.epl.col[2], c2 = a.epl.col[3];
+  for (int b = threadIdx.x; b < a.bs; b += kThreads) {
+    const int im = a.img_id ? a.img_id[b] : 0;
+    const float e1 = c1 >= 0 ? a.x[(size_t)b * a.d + c1] : 0.f;
+    const float e2 = c2 >= 0 ? a.x[(size_t)b * a.d + c2] : 0.f;
+    const float f = epl_f_of(e1, e2);
+    for (int i = 0; i < GL_MAX_IMAGES; ++i)
+      if (i == im) mx[i] = fmaxf(mx[i], f);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = 0; i < a.n_images; ++i) {
+    float m = mx[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) st.red[warp][i & 3] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      for (int w = 0; w < kThreads / 32; ++w) t = fmaxf(t, st.red[w][i & 3]);
+      st.K[i] = epl_terms_from_maxf(t, a.epl.niter);
+    }
+    __syncthreads();
+  }
+}
+
+// Correlation of one band: output rows [i0, i0+nb) of channel slot cc.
+template <int KS>
+__device__ void lsq_band_conv(const LsqImage& I, const float* sm, int cc, int nb, int i0,
+                              float* __restrict__ Xout /* X[b][c] base */) {
+  const int units = nb * I.ncb;
+  for (int u = threadIdx.x; u < units * I.CPn; u += kThreads) {
+    const int slot = u / units;
+    if (slot + cc >= I.cpass) continue;
+    const int uu = u - slot * units;
+    const int il = uu / I.ncb, cb = uu - il * I.ncb;
+    const int j0 = kColBlock * cb;
+    if (j0 >= I.N) continue;
+    float acc[kColBlock];
+#pragma unroll
+    for (int c = 0; c < kColBlock; ++c) acc[c] = 0.f;
+    for (int pq = 0; pq < I.nplanes; ++pq) {
+      const int q = pq - (pq / I.ss) * I.ss;
+      const float* plane = sm + I.offP + (slot * I.nplanes + pq) * I.brows * I.pitch + I.padI[q] - I.d[q] + j0;
+      const float* kp = sm + I.offK + pq * KS * I.ksp;
+#pragma unroll 1
+      for (int m = 0; m < KS; ++m) corr_row<KS, false>(plane + (il + m) * I.pitch, kp + m * I.ksp, acc);
+    }
+    float* dst = Xout + (size_t)(cc + slot) * I.xcstride + (size_t)(i0 + il) * I.N + j0;
+#pragma unroll
+    for (int c = 0; c < kColBlock; ++c)
+      if (j0 + c < I.N) dst[c] = acc[c];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_constant__ LsqArgs a) {
+  extern __shared__ float4 smem_dyn[];
+  float* sm = reinterpret_cast<float*>(smem_dyn);
+  __shared__ LsqShared st;
+  __shared__ float pref[kMaxShapeletN + 1];
+  const int tid = threadIdx.x;
+  if (tid <= kMaxShapeletN) {
+    double f = 1.0;
+    for (int i = 2; i <= tid; ++i) f *= i;
+    pref[tid] = (float)(1.0 / sqrt(pow(2.0, tid) * sqrt(3.14159265358979323846) * f));
+  }
+  lsq_term_counts(a, st);
+  const int total = a.bs * a.max_bands;
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    const int b = item / a.max_bands, band = item - b * a.max_bands;
+    const int im = a.img_id ? a.img_id[b] : 0;
+    if (im < 0 || im >= a.n_images) continue;
+    const LsqImage& I = a.img[im];
+    if (band >= I.nbands) continue;
+    const int i0 = band * I.Bo;
+    const int nb = min(I.Bo, I.N - i0);
+    const int Ylo = i0 - I.d[0];            // plane row of band row 0
+    if (tid < a.d) st.x[tid] = a.x[(size_t)b * a.d + tid];
+    // zero planes (rows outside the image stay zero), load sub-kernels
+    for (int i = tid; i < I.offK; i += kThreads) sm[i] = 0.f;
+    for (int i = tid; i < I.nplanes * I.KS * I.ksp; i += kThreads) sm[I.offK + i] = __ldg(I.kern + i);
+    __syncthreads();
+    const int K = st.K[im];
+    const int* e = a.epl.col;
+    if (tid < 32) {
+      const float f = epl_f_of(lpget(st.x, e[2], 0.f), lpget(st.x, e[3], 0.f));
+      const float t = lpget(st.x, e[1], 2.f) - 1.f;
+      float carry = 0.f;
+      for (int base = 1; base <= K; base += 32) {
+        const int n = base + tid;
+        float dl = (n <= K) ? epl_dlnp_dt(t, n) : 0.f;
+        for (int o = 1; o < 32; o <<= 1) {
+          const float y = __shfl_up_sync(0xffffffffu, dl, o);
+          if (tid >= o) dl += y;
+        }
+        if (n <= K) st.tab[n] = make_float2(epl_prefac(f, t, n), carry + dl);
+        carry += __shfl_sync(0xffffffffu, dl, 31);
+      }
+    }
+    __syncthreads();
+    // ray-trace the band: beta per (plane, band row, column)
+    {
+      const EplC ec = epl_consts(lpget(st.x, e[0], 0.f), lpget(st.x, e[1], 2.f), lpget(st.x, e[2], 0.f),
+                                 lpget(st.x, e[3], 0.f), lpget(st.x, e[4], 0.f), lpget(st.x, e[5], 0.f), K);
+      const float g1 = a.has_shear ? lpget(st.x, a.shear.col[0], 0.f) : 0.f;
+      const float g2 = a.has_shear ? lpget(st.x, a.shear.col[1], 0.f) : 0.f;
+      const float2* grid = reinterpret_cast<const float2*>(I.grid);
+      float2* beta = reinterpret_cast<float2*>(sm + I.offB);
+      const int per_plane = I.brows * I.N;
+      for (int v = tid; v < I.nplanes * per_plane; v += kThreads) {
+        const int pq = v / per_plane;
+        const int r = v - pq * per_plane;
+        const int yr = r / I.N, X = r - yr * I.N;
+        const int Y = Ylo + yr;
+        float2 bt = make_float2(0.f, 0.f);
+        if (Y >= 0 && Y < I.N) {
+          const float2 xy = __ldg(grid + ((size_t)pq * I.N + Y) * I.N + X);
+          float ax, ay;
+          epl_deflect(ec, st.tab, xy.x, xy.y, ax, ay);
+          bt.x = xy.x - ax;
+          bt.y = xy.y - ay;
+          if (a.has_shear) {
+            bt.x = bt.x - (g1 * xy.x + g2 * xy.y);
+            bt.y = bt.y - (g2 * xy.x - g1 * xy.y);
+          }
+        }
+        beta[v] = bt;
+      }
+    }
+    __syncthreads();
+    float* Xb = a.X + (size_t)b * a.xstride;
+    for (int c0 = 0; c0 < a.D; c0 += I.CPn) {
+      // evaluate channels c0 .. c0+CPn-1 on the band
+      const int per_plane = I.brows * I.N;
+      const float2* beta = reinterpret_cast<const float2*>(sm + I.offB);
+      const float2* grid = reinterpret_cast<const float2*>(I.grid);
+      for (int v = tid; v < I.CPn * I.nplanes * per_plane; v += kThreads) {
+        const int slot = v / (I.nplanes * per_plane);
+        const int c = c0 + slot;
+        if (c >= a.D) continue;
+        const int vv = v - slot * I.nplanes * per_plane;
+        const int pq = vv / per_plane;
+        const int r = vv - pq * per_plane;
+        const int yr = r / I.N, X = r - yr * I.N;
+        const int Y = Ylo + yr;
+        if (Y < 0 || Y >= I.N) continue;   // stays zero
+        const int q = pq - (pq / I.ss) * I.ss;
+        const LsqChannel ch = a.ch[c];
+        const LsqProfile& pr = a.prof[ch.prof];
+        float px, py;
+        if (pr.group == GL_GROUP_SOURCE) {
+          const float2 bt = beta[vv];
+          px = bt.x;
+          py = bt.y;
+        } else {
+          const float2 xy = __ldg(grid + ((size_t)pq * I.N + Y) * I.N + X);
+          px = xy.x;
+          py = xy.y;
+        }
+        float val;
+        if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
+          const float bs_ = lpget(st.x, pr.col[0], 1.f);
+          const float u = (px - lpget(st.x, pr.col[1], 0.f)) / bs_;
+          const float w = (py - lpget(st.x, pr.col[2], 0.f)) / bs_;
+          const float fac = expf(-(u * u + w * w) / 2.f);
+          val = fac * hermite_fn(ch.n1, u, pref) * hermite_fn(ch.n2, w, pref);
+        } else {              // unit-amplitude Sersic
+          const SerC s = sersic_consts(lpget(st.x, pr.col[0], 1.f), lpget(st.x, pr.col[1], 1.f),
+                                       lpget(st.x, pr.col[2], 0.f), lpget(st.x, pr.col[3], 0.f),
+                                       lpget(st.x, pr.col[4], 0.f), lpget(st.x, pr.col[5], 0.f), 1.f);
+          val = sersic_light(s, px, py);
+        }
+        if (isnan(val)) val = 0.f;
+        sm[I.offP + (slot * I.nplanes + pq) * I.brows * I.pitch + yr * I.pitch + I.padI[q] + X] = val;
+      }
+      __syncthreads();
+#define GL_CALL_LSQ(KSV) lsq_band_conv<KSV>(I, sm, c0, nb, i0, Xb)
+      GL_KS_DISPATCH(I.KS, GL_CALL_LSQ)
+#undef GL_CALL_LSQ
+      __syncthreads();
+    }
+  }
+}
+
+// G_b = X^T W^2 X (upper triangle mirrored), h_b = X^T W^2 y.
+__global__ void __launch_bounds__(256) lsq_gram_kernel(const __grid_constant__ LsqArgs a, float* G,
+                                                       float* h) {
+  __shared__ float xs[kMaxLsqChannels][33];
+  __shared__ float ws[32], ys[32];
+  const int D = a.D;
+  const int ntri = D * (D + 1) / 2;
+  for (int b = blockIdx.x; b < a.bs; b += gridDim.x) {
+    const int im = a.img_id ? a.img_id[b] : 0;
+    if (im < 0 || im >= a.n_images) continue;
+    const LsqImage& I = a.img[im];
+    const int P = I.N * I.N;
+    const float* Xb = a.X + (size_t)b * a.xstride;
+    // entries e = tid + k*256 of the upper triangle (then h): decode (i, j) once
+    constexpr int kMaxE = (kMaxLsqChannels * (kMaxLsqChannels + 1) / 2 + kMaxLsqChannels + 255) / 256;
+    float accv[kMaxE];
+    int ei[kMaxE], ej[kMaxE];
+#pragma unroll
+    for (int k = 0; k < kMaxE; ++k) {
+      accv[k] = 0.f;
+      const int e = threadIdx.x + 256 * k;
+      int i = -1, j = -1;
+      if (e < ntri) {
+        int rem = e;
+        i = 0;
+        while (rem >= D - i) {
+          rem -= D - i;
+          ++i;
+        }
+        j = i + rem;
+      } else if (e < ntri + D) {
+        i = e - ntri;
+        j = -2;   // h entry
+      }
+      ei[k] = i;
+      ej[k] = j;
+    }
+    for (int p0 = 0; p0 < P; p0 += 32) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < 32; t += blockDim.x) {
+        const int p = p0 + t;
+        const float w = (p < P) ? 1.f / I.err[p] : 0.f;
+        ws[t] = w;
+        ys[t] = (p < P) ? I.obs[p] * w : 0.f;
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < D * 32; t += blockDim.x) {
+        const int c = t >> 5, pp = t & 31;
+        const int p = p0 + pp;
+        xs[c][pp] = (p < P) ? Xb[(size_t)c * I.xcstride + p] * ws[pp] : 0.f;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kMaxE; ++k) {
+        const int i = ei[k], j = ej[k];
+        if (i < 0) continue;
+        const float* xj = (j >= 0) ? xs[j] : ys;
+        float s = 0.f;
+#pragma unroll 8
+        for (int pp = 0; pp < 32; ++pp) s = fmaf(xs[i][pp], xj[pp], s);
+        accv[k] += s;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxE; ++k) {
+      const int i = ei[k], j = ej[k];
+      if (i < 0) continue;
+      if (j >= 0) {
+        G[((size_t)b * D + i) * D + j] = accv[k];
+        G[((size_t)b * D + j) * D + i] = accv[k];
+      } else {
+        h[(size_t)b * D + i] = accv[k];
+      }
+    }
+  }
+}
+
+// pinv(G) h by cyclic Jacobi (round-robin parallel ordering), one CTA per sample.
+__global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const float* __restrict__ G,
+                                                        const float* __restrict__ h, float rcond,
+                                                        float* __restrict__ coeffs, int max_sweeps) {
+  __shared__ float A[kMaxLsqChannels + 1][kMaxLsqChannels + 1];
+  __shared__ float V[kMaxLsqChannels + 1][kMaxLsqChannels + 1];
+  __shared__ float cs[kMaxLsqChannels / 2 + 1][2];
+  __shared__ int pr[kMaxLsqChannels / 2 + 1][2];
+  __shared__ float hs[kMaxLsqChannels + 1];
+  __shared__ float red[2];
+  const int n = (D + 1) & ~1;   // even size; a padding index carries a zero row/column
+  const int npair = n / 2;
+  for (int b = blockIdx.x; b < bs; b += gridDim.x) {
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const int i = t / n, j = t - i * n;
+      A[i][j] = (i < D && j < D) ? G[((size_t)b * D + i) * D + j] : 0.f;
+      V[i][j] = (i == j) ? 1.f : 0.f;
+    }
+    for (int t = threadIdx.x; t < n; t += blockDim.x) hs[t] = (t < D) ? h[(size_t)b * D + t] : 0.f;
+    __syncthreads();
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+      // convergence test: off-diagonal vs diagonal Frobenius norm (block reduction)
+      {
+        float off = 0.f, dg = 0.f;
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+          const int i = t / n, j = t - i * n;
+          const float v = A[i][j] * A[i][j];
+          if (i == j) dg += v;
+          else off += v;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          off += __shfl_xor_sync(0xffffffffu, off, o);
+          dg += __shfl_xor_sync(0xffffffffu, dg, o);
+        }
+        __shared__ float wred[2][4];
+        if ((threadIdx.x & 31) == 0) {
+          wred[0][threadIdx.x >> 5] = off;
+          wred[1][threadIdx.x >> 5] = dg;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          red[0] = wred[0][0] + wred[0][1] + wred[0][2] + wred[0][3];
+          red[1] = wred[1][0] + wred[1][1] + wred[1][2] + wred[1][3];
+        }
+        __syncthreads();
+      }
+      const bool done = !(red[0] > 1e-13f * red[1]);
+      __syncthreads();
+      if (done) break;
+      for (int round = 0; round < n - 1; ++round) {
+        // tournament pairing: index 0 fixed, the others rotate
+        if (threadIdx.x < npair) {
+          const int k = threadIdx.x;
+          int p, q;
+          auto at = [&](int pos) { return pos == 0 ? 0 : 1 + ((pos - 1 + round) % (n - 1)); };
+          p = at(k);
+          q = at(n - 1 - k);
+          if (p > q) {
+            const int t = p;
+            p = q;
+            q = t;
+          }
+          const float apq = A[p][q];
+          float c = 1.f, s = 0.f;
+          if (fabsf(apq) > 1e-30f) {
+            const float theta = (A[q][q] - A[p][p]) / (2.f * apq);
+            const float t = copysignf(1.f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.f));
+            c = rsqrtf(t * t + 1.f);
+            s = t * c;
+          }
+          cs[k][0] = c;
+          cs[k][1] = s;
+          pr[k][0] = p;
+          pr[k][1] = q;
+        }
+        __syncthreads();
+        // rows: A <- J^T A
+        for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
+          const int k = t / n, j = t - k * n;
+          const int p = pr[k][0], q = pr[k][1];
+          const float c = cs[k][0], s = cs[k][1];
+          const float ap = A[p][j], aq = A[q][j];
+          A[p][j] = c * ap - s * aq;
+          A[q][j] = s * ap + c * aq;
+        }
+        __syncthreads();
+        // columns: A <- A J, V <- V J
+        for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
+          const int k = t / n, i = t - k * n;
+          const int p = pr[k][0], q = pr[k][1];
+          const float c = cs[k][0], s = cs[k][1];
+          const float ap = A[i][p], aq = A[i][q];
+          A[i][p] = c * ap - s * aq;
+          A[i][q] = s * ap + c * aq;
+          const float vp = V[i][p], vq = V[i][q];
+          V[i][p] = c * vp - s * vq;
+          V[i][q] = s * vp + c * vq;
+        }
+        __syncthreads();
+      }
+    }
+    // pinv solve: coeffs = sum over kept eigenpairs of (v_i . h / lambda_i) v_i
+    if (threadIdx.x == 0) {
+      float m = 0.f;
+      for (int i = 0; i < D; ++i) m = fmaxf(m, fabsf(A[i][i]));
+      red[0] = rcond * m;
+    }
+    __syncthreads();
+    const float cutoff = red[0];
+    // proj_i = (v_i . h) / lambda_i, reuse cs[][0] as storage when n/2 >= D is false -> use hs tail
+    __shared__ float proj[kMaxLsqChannels + 1];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      float s = 0.f;
+      for (int r = 0; r < n; ++r) s = fmaf(V[r][i], hs[r], s);
+      const float lam = A[i][i];
+      proj[i] = (i < D && fabsf(lam) > cutoff) ? s / lam : 0.f;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < D; r += blockDim.x) {
+      float s = 0.f;
+      for (int i = 0; i < n; ++i) s = fmaf(V[r][i], proj[i], s);
+      coeffs[(size_t)b * D + r] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// img = sum_c coeffs_c X_c; BackwardProbModel likelihood with the data error map.
+__global__ void __launch_bounds__(256) lsq_image_kernel(const __grid_constant__ LsqArgs a,
+                                                        const float* __restrict__ coeffs,
+                                                        float* img_out, float* logL, float* chi2) {
+  __shared__ float cf[kMaxLsqChannels];
+  __shared__ float red[2][8];
+  for (int b = blockIdx.x; b < a.bs; b += gridDim.x) {
+    const int im = a.img_id ? a.img_id[b] : 0;
+    if (im < 0 || im >= a.n_images) continue;
+    const LsqImage& I = a.img[im];
+    const int P = I.N * I.N;
+    for (int c = threadIdx.x; c < a.D; c += blockDim.x) cf[c] = coeffs[(size_t)b * a.D + c];
+    __syncthreads();
+    const float* Xb = a.X + (size_t)b * a.xstride;
+    float ls = 0.f, cs2 = 0.f;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+      float v = 0.f;
+      for (int c = 0; c < a.D; ++c) v = fmaf(Xb[(size_t)c * I.xcstride + p], cf[c], v);
+      if (img_out) img_out[(size_t)b * a.maxP + p] = v;
+      if (I.obs) {
+        const float err = I.err[p];
+        const float zz = (v - I.obs[p]) / err;
+        ls += -0.5f * zz * zz - logf(err) - kHalfLog2Pi;
+        cs2 += zz * zz;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      ls += __shfl_xor_sync(0xffffffffu, ls, o);
+      cs2 += __shfl_xor_sync(0xffffffffu, cs2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[0][threadIdx.x >> 5] = ls;
+      red[1][threadIdx.x >> 5] = cs2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float l = 0.f, c = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        l += red[0][w];
+        c += red[1][w];
+      }
+      if (logL) logL[b] = l;
+      if (chi2) chi2[b] = c / (float)P;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ host side
+static int g_lsq_smem_set = -1;
+
+int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
+  LsqPlan* L = new LsqPlan;
+  memset(L, 0, sizeof(*L));
+  const gl_model_desc& m = plan->model;
+  int D = 0;
+  for (int i = 0; i < m.n_profiles; ++i) {
+    const gl_profile_desc& p = m.prof[i];
+    if (p.group == GL_GROUP_LENS) {
+      if (p.type == GL_PROF_EPL) {
+        L->epl.type = p.type;
+        L->epl.niter = p.niter;
+        for (int k = 0; k < GL_MAX_PROFILE_PARAMS; ++k) L->epl.col[k] = p.col[k];
+      } else if (p.type == GL_PROF_SHEAR) {
+        L->has_shear = 1;
+        for (int k = 0; k < GL_MAX_PROFILE_PARAMS; ++k) L->shear.col[k] = p.col[k];
+      }
+      continue;
+    }
+    if (L->n_prof >= kMaxLsqProfiles) {
+      set_error("least squares: at most %d light profiles", kMaxLsqProfiles);
+      delete L;
+      return GL_ERR_UNSUPPORTED;
+    }
+    LsqProfile& pr = L->prof[L->n_prof];
+    pr.group = p.group;
+    pr.type = p.type;
+    for (int k = 0; k < GL_MAX_PROFILE_PARAMS; ++k) pr.col[k] = -1;
+    if (p.type == GL_PROF_SHAPELETS) {
+      if (p.niter < 0 || p.niter > kMaxShapeletN) {
+        set_error("shapelets n_max %d outside [0, %d]", p.niter, kMaxShapeletN);
+        delete L;
+        return GL_ERR_UNSUPPORTED;
+      }
+      for (int k = 0; k < 3; ++k) pr.col[k] = p.col[k];
+      int n1 = 0, n2 = 0;
+      const int nl = (p.niter + 1) * (p.niter + 2) / 2;
+      for (int k = 0; k < nl; ++k) {
+        if (D >= kMaxLsqChannels) break;
+        L->ch[D].kind = 1;
+        L->ch[D].prof = L->n_prof;
+        L->ch[D].n1 = n1;
+        L->ch[D].n2 = n2;
+        ++D;
+        if (n1 == 0) {
+          n1 = n2 + 1;
+          n2 = 0;
+        } else {
+          --n1;
+          ++n2;
+        }
+      }
+    } else if (p.type == GL_PROF_SERSIC_ELLIPSE || p.type == GL_PROF_SERSIC) {
+      if (p.type == GL_PROF_SERSIC_ELLIPSE) {
+        for (int k = 0; k < 6; ++k) pr.col[k] = p.col[k];
+      } else {
+        pr.col[0] = p.col[0];
+        pr.col[1] = p.col[1];
+        pr.col[4] = p.col[2];
+        pr.col[5] = p.col[3];
+      }
+      if (D >= kMaxLsqChannels) break;
+      L->ch[D].kind = 0;
+      L->ch[D].prof = L->n_prof;
+      ++D;
+    } else {
+      set_error("least squares: light type %d not supported", p.type);
+      delete L;
+      return GL_ERR_UNSUPPORTED;
+    }
+    if (!p.use_lstsq) {
+      set_error("least squares needs every light profile with use_lstsq");
+      delete L;
+      return GL_ERR_UNSUPPORTED;
+    }
+    ++L->n_prof;
+  }
+  if (L->epl.type != GL_PROF_EPL || D < 1 || D > kMaxLsqChannels) {
+    set_error("least squares needs an EPL lens and 1..%d basis channels (got %d)", kMaxLsqChannels, D);
+    delete L;
+    return GL_ERR_UNSUPPORTED;
+  }
+  L->D = D;
+  int dev_smem = 0;
+  cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
+  const int static_bytes = 8 * 1024;
+  int maxP = 0, smem = 0, max_bands = 0;
+  for (int i = 0; i < plan->n_images; ++i) {
+    const DevImage& F = plan->img[i];
+    LsqImage& I = L->img[i];
+    I.N = F.N;
+    I.ss = F.ss;
+    I.nplanes = F.nplanes;
+    I.KS = F.KS;
+    I.ksp = F.ksp;
+    for (int k = 0; k < kMaxPlanes; ++k) {
+      I.d[k] = F.d[k];
+      I.padI[k] = F.padI[k];
+    }
+    I.ncb = ((F.N + kColBlock - 1) / kColBlock);
+    I.pitch = F.pitchI;
+    I.grid = F.grid;
+    I.kern = F.kern;
+    I.obs = F.obs;
+    I.xcstride = F.N * F.N;
+    // band height and channels per pass: use the most threads that fit
+    int best_score = -1;
+    for (int cp = 2; cp >= 1; --cp)
+      for (int bo = F.N; bo >= 1; --bo) {
+        const int brows = bo + F.KS - 1;
+        const int fl = 2 * F.nplanes * brows * F.N + cp * F.nplanes * brows * F.pitchI +
+                       F.nplanes * F.KS * F.ksp;
+        if (fl * 4 + static_bytes > dev_smem) continue;
+        const int units = bo * I.ncb * cp;
+        const int rounds = (units + kThreads - 1) / kThreads;
+        const int nbands = (F.N + bo - 1) / bo;
+        // score: thread utilisation of the correlation and halo overhead
+        const double util = (double)units / (rounds * kThreads);
+        const double halo = (double)bo / brows;
+        const int score = (int)(1e6 * util * halo * (cp == 2 ? 1.0 : 0.9));
+        if (score > best_score) {
+          best_score = score;
+          I.Bo = bo;
+          I.CPn = cp;
+          I.brows = brows;
+          I.nbands = nbands;
+        }
+        break;   // the largest band for this cp
+      }
+    if (best_score < 0) {
+      set_error("least squares: image %d does not fit in shared memory", i);
+      delete L;
+      return GL_ERR_UNSUPPORTED;
+    }
+    // refine: among band heights that fit, pick the best utilisation
+    for (int bo = I.Bo; bo >= 4; --bo) {
+      const int units = bo * I.ncb * I.CPn;
+      const int rounds = (units + kThreads - 1) / kThreads;
+      const double util = (double)units / (rounds * kThreads);
+      const double halo = (double)bo / (bo + F.KS - 1);
+      const int score = (int)(1e6 * util * halo * (I.CPn == 2 ? 1.0 : 0.9));
+      if (score > best_score) {
+        best_score = score;
+        I.Bo = bo;
+        I.brows = bo + F.KS - 1;
+        I.nbands = (F.N + bo - 1) / bo;
+      }
+    }
+    I.cpass = D;
+    I.offB = 0;
+    I.offP = 2 * F.nplanes * I.brows * F.N;
+    I.offP = (I.offP + 3) & ~3;
+    I.offK = I.offP + I.CPn * F.nplanes * I.brows * F.pitchI;
+    I.smem_floats = I.offK + F.nplanes * F.KS * F.ksp;
+    if (I.smem_floats * 4 > smem) smem = I.smem_floats * 4;
+    if (F.N * F.N > maxP) maxP = F.N * F.N;
+    if (I.nbands > max_bands) max_bands = I.nbands;
+  }
+  L->smem_bytes = smem;
+  L->maxP = maxP;
+  L->max_bands = max_bands;
+  // error maps on the device
+  size_t bytes = 0;
+  for (int i = 0; i < plan->n_images; ++i) bytes += ((size_t)errs[i].size() * 4 + 255) / 256 * 256;
+  if (cudaMalloc((void**)&L->dev_err, bytes) != cudaSuccess) {
+    set_error("cudaMalloc(error maps) failed");
+    delete L;
+    return GL_ERR_NOMEM;
+  }
+  char* base = (char*)L->dev_err;
+  for (int i = 0; i < plan->n_images; ++i) {
+    cudaMemcpy(base, errs[i].data(), errs[i].size() * 4, cudaMemcpyHostToDevice);
+    L->img[i].err = (const float*)base;
+    base += ((size_t)errs[i].size() * 4 + 255) / 256 * 256;
+  }
+  if (smem > g_lsq_smem_set) {
+    cudaError_t e = cudaFuncSetAttribute(lsq_basis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) {
+      set_error("lsq smem attribute: %s", cudaGetErrorString(e));
+      cudaFree(L->dev_err);
+      delete L;
+      return GL_ERR_CUDA;
+    }
+    g_lsq_smem_set = smem;
+  }
+  plan->lsq = L;
+  return GL_OK;
+}
+
+void lsq_destroy(gl_plan* plan) {
+  if (!plan->lsq) return;
+  LsqPlan* L = (LsqPlan*)plan->lsq;
+  if (L->dev_err) cudaFree(L->dev_err);
+  delete L;
+  plan->lsq = nullptr;
+}
+
+size_t lsq_workspace_bytes(const LsqPlan* L, int bs) {
+  const size_t X = (size_t)bs * L->D * L->maxP * 4;
+  const size_t G = (size_t)bs * L->D * L->D * 4;
+  const size_t h = (size_t)bs * L->D * 4;
+  return ((X + 255) / 256 + (G + 255) / 256 + (h + 255) / 256) * 256;
+}
+
+int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, float* work,
+            size_t work_bytes, float* coeffs, float* img_out, float* logL, float* chi2,
+            cudaStream_t stream) {
+  const LsqPlan* L = (const LsqPlan*)plan->lsq;
+  if (work_bytes < lsq_workspace_bytes(L, bs)) {
+    set_error("least squares workspace too small: %zu < %zu bytes", work_bytes, lsq_workspace_bytes(L, bs));
+    return GL_ERR_INVALID;
+  }
+  if (bs == 0) return GL_OK;
+  LsqArgs a;
+  memset(&a, 0, sizeof(a));
+  a.bs = bs;
+  a.d = plan->model.n_params;
+  a.D = L->D;
+  a.n_images = plan->n_images;
+  a.n_prof = L->n_prof;
+  for (int i = 0; i < kMaxLsqProfiles; ++i) a.prof[i] = L->prof[i];
+  for (int i = 0; i < kMaxLsqChannels; ++i) a.ch[i] = L->ch[i];
+  a.epl = L->epl;
+  a.shear = L->shear;
+  a.has_shear = L->has_shear;
+  for (int i = 0; i < plan->n_images; ++i) a.img[i] = L->img[i];
+  a.x = x;
+  a.img_id = img_id;
+  a.maxP = L->maxP;
+  a.max_bands = L->max_bands;
+  a.xstride = (size_t)L->D * L->maxP;
+  char* base = (char*)work;
+  a.X = (float*)base;
+  base += (((size_t)bs * L->D * L->maxP * 4 + 255) / 256) * 256;
+  float* G = (float*)base;
+  base += (((size_t)bs * L->D * L->D * 4 + 255) / 256) * 256;
+  float* h = (float*)base;
+  int sms = 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
+  const int items = bs * L->max_bands;
+  lsq_basis_kernel<<<items < sms ? items : sms, kThreads, L->smem_bytes, stream>>>(a);
+  lsq_gram_kernel<<<bs < 4 * sms ? bs : 4 * sms, 256, 0, stream>>>(a, G, h);
+  float* co = coeffs;
+  if (!co) {
+    set_error("least squares: coeffs buffer required");
+    return GL_ERR_INVALID;
+  }
+  lsq_solve_kernel<<<bs < 8 * sms ? bs : 8 * sms, 128, 0, stream>>>(bs, L->D, G, h, 1e-6f, co, 30);
+  if (img_out || logL || chi2)
+    lsq_image_kernel<<<bs < 4 * sms ? bs : 4 * sms, 256, 0, stream>>>(a, co, img_out, logL, chi2);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("least squares launch: %s", cudaGetErrorString(e));
+    return GL_ERR_CUDA;
+  }
+  return GL_OK;
+}
+
+}  // namespace gl

@@ -1,0 +1,71 @@
+// Structures of the linear-amplitude (least-squares) path; see gl_lstsq.cu.
+#pragma once
+#include <cstddef>
+#include <vector>
+
+#include "gl_internal.cuh"
+
+namespace gl {
+
+constexpr int kMaxLsqChannels = 64;   // basis images per sample (shapelets n_max <= 9 + lens light)
+constexpr int kMaxLsqProfiles = 4;
+constexpr int kMaxShapeletN = 9;
+
+struct LsqChannel {
+  int kind;    // 0: unit-amplitude Sersic, 1: shapelet basis function
+  int prof;    // light-profile slot
+  int n1, n2;  // shapelet orders
+};
+
+struct LsqProfile {
+  int type, group;
+  int col[GL_MAX_PROFILE_PARAMS];  // SHAPELETS: beta, cx, cy; Sersic: SERSIC_ELLIPSE slots
+};
+
+struct LsqImage {
+  int N, ss, nplanes, KS, ksp;
+  int d[kMaxPlanes], padI[kMaxPlanes];
+  int ncb, pitch;
+  int Bo;      // output rows per band
+  int CPn;     // channels per correlation pass
+  int brows;   // plane rows per band (Bo + KS - 1)
+  int nbands;
+  int cpass;   // number of channels (D)
+  int xcstride;   // floats between channels in X (N*N)
+  int offB, offP, offK, smem_floats;
+  const float* grid;
+  const float* kern;
+  const float* obs;
+  const float* err;
+};
+
+struct LsqArgs {
+  int bs, d, D, n_images, n_prof, has_shear;
+  int maxP, max_bands;
+  size_t xstride;   // floats per sample in X
+  LsqProfile prof[kMaxLsqProfiles];
+  LsqChannel ch[kMaxLsqChannels];
+  DevProfile epl, shear;
+  LsqImage img[GL_MAX_IMAGES];
+  const float* x;
+  const int* img_id;
+  float* X;
+};
+
+struct LsqPlan {
+  int D, n_prof, has_shear, maxP, max_bands, smem_bytes;
+  LsqProfile prof[kMaxLsqProfiles];
+  LsqChannel ch[kMaxLsqChannels];
+  DevProfile epl, shear;
+  LsqImage img[GL_MAX_IMAGES];
+  float* dev_err;
+};
+
+int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs);
+void lsq_destroy(gl_plan* plan);
+size_t lsq_workspace_bytes(const LsqPlan* L, int bs);
+int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, float* work,
+            size_t work_bytes, float* coeffs, float* img_out, float* logL, float* chi2,
+            cudaStream_t stream);
+
+}  // namespace gl

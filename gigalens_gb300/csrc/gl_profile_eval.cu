@@ -90,6 +90,51 @@ int launch_profile_eval(int type, const float* x, const float* y, int64_t n, con
   return GL_OK;
 }
 
+// Shapelets at n points: Hermite recursion per point, all orders at once.
+__global__ void shapelets_eval_kernel(int n_max, const float* __restrict__ x, const float* __restrict__ y,
+                                      int64_t n, const float* __restrict__ prm, const float* __restrict__ amps,
+                                      float* __restrict__ out) {
+  __shared__ float pref[32];
+  if (threadIdx.x <= n_max) {
+    double f = 1.0;
+    for (int i = 2; i <= (int)threadIdx.x; ++i) f *= i;
+    pref[threadIdx.x] = (float)(1.0 / sqrt(pow(2.0, (double)threadIdx.x) * sqrt(3.14159265358979323846) * f));
+  }
+  __syncthreads();
+  const int D = (n_max + 1) * (n_max + 2) / 2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float beta = prm[i], cx = prm[n + i], cy = prm[2 * n + i];
+    const float u = (x[i] - cx) / beta, v = (y[i] - cy) / beta;
+    float hu[32], hv[32];
+    hu[0] = 1.f;
+    hv[0] = 1.f;
+    if (n_max >= 1) {
+      hu[1] = 2.f * u;
+      hv[1] = 2.f * v;
+    }
+    for (int k = 2; k <= n_max; ++k) {
+      hu[k] = 2.f * (u * hu[k - 1] - (float)(k - 1) * hu[k - 2]);
+      hv[k] = 2.f * (v * hv[k - 1] - (float)(k - 1) * hv[k - 2]);
+    }
+    const float fac = expf(-(u * u + v * v) / 2.f);
+    float acc = 0.f;
+    int n1 = 0, n2 = 0;
+    for (int k = 0; k < D; ++k) {
+      const float bk = fac * (hu[n1] * pref[n1]) * (hv[n2] * pref[n2]);
+      if (amps) acc = fmaf(amps[(int64_t)k * n + i], bk, acc);
+      else out[(int64_t)k * n + i] = bk;
+      if (n1 == 0) {
+        n1 = n2 + 1;
+        n2 = 0;
+      } else {
+        --n1;
+        ++n2;
+      }
+    }
+    if (amps) out[i] = acc;
+  }
+}
+
 // One block: max over the batch of f, then the reference's term-count rule.
 __global__ void epl_term_count_kernel(const float* __restrict__ e1, const float* __restrict__ e2,
                                       int64_t n, int cap, int* __restrict__ k_out) {
@@ -105,6 +150,20 @@ __global__ void epl_term_count_kernel(const float* __restrict__ e1, const float*
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmaxf(t, red[w]);
     *k_out = epl_terms_from_maxf(t, cap);
   }
+}
+
+int launch_shapelets_eval(int n_max, const float* x, const float* y, int64_t n, const float* params,
+                          const float* amps, float* out, cudaStream_t stream) {
+  if (n == 0) return GL_OK;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  shapelets_eval_kernel<<<(int)blocks, 256, 0, stream>>>(n_max, x, y, n, params, amps, out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("shapelets launch: %s", cudaGetErrorString(e));
+    return GL_ERR_CUDA;
+  }
+  return GL_OK;
 }
 
 int launch_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out,

@@ -99,7 +99,7 @@ class ModelLayout:
         return out.contiguous()
 
 
-def image_desc(sim_config: SimulatorConfig, observed=None, background_rms=1.0, exp_time=1.0):
+def image_desc(sim_config: SimulatorConfig, observed=None, background_rms=1.0, exp_time=1.0, err_map=None):
     """Fill a ``gl_image_desc``; returns (desc, keep-alive host arrays)."""
     g = N.gl_image_desc()
     g.num_pix = int(sim_config.num_pix)
@@ -127,6 +127,14 @@ def image_desc(sim_config: SimulatorConfig, observed=None, background_rms=1.0, e
         g.observed = None
     g.background_rms = float(background_rms)
     g.exp_time = float(exp_time)
+    if err_map is not None:
+        e = np.ascontiguousarray(np.asarray(err_map, dtype=np.float32))
+        if e.shape != (g.num_pix, g.num_pix):
+            raise ValueError("err_map shape %s != (%d, %d)" % (e.shape, g.num_pix, g.num_pix))
+        keep.append(e)
+        g.err_map = e.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    else:
+        g.err_map = None
     return g, keep
 
 

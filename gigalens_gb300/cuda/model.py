@@ -71,3 +71,62 @@ class ForwardProbModel(_model.ProbabilisticModel):
         if z.dim() == 1:
             z = z[None]
         return _LogProb.apply(z, plan, None)
+
+
+class _LstsqLogL(torch.autograd.Function):
+    """Likelihood of the least-squares image: value by ``gl_lstsq``."""
+
+    @staticmethod
+    def forward(ctx, x, simulator, plan):
+        r = simulator.run_lstsq(plan, x.detach(), want_image=False, want_loglik=True)
+        ctx.mark_non_differentiable(r["chi2"])
+        ctx.simulator, ctx.plan = simulator, plan
+        ctx.save_for_backward(x.detach(), r["coeffs"])
+        return r["logL"], r["chi2"]
+
+    @staticmethod
+    def backward(ctx, g_logL, g_chi2):
+        x, coeffs = ctx.saved_tensors
+        grad = ctx.simulator.lstsq_loglik_grad(ctx.plan, x, coeffs)
+        return grad * g_logL.unsqueeze(1), None, None
+
+
+class BackwardProbModel(_model.ProbabilisticModel):
+    """Log posterior with the observed image as the noise estimator and the
+    linear light amplitudes solved by least squares (``tf/model.py:89-163``).
+
+    ``fldj_of_x`` keeps the reference's TensorFlow behaviour of evaluating the
+    bijector's log-Jacobian at the physical parameters x (``tf/model.py:160``);
+    ``False`` evaluates it at the unconstrained z, as the JAX substrate does
+    (``jax/model.py:77``)."""
+
+    def __init__(self, prior, observed_image, background_rms, exp_time, fldj_of_x=True):
+        super().__init__(prior)
+        obs = observed_image.detach().cpu().numpy() if torch.is_tensor(observed_image) else observed_image
+        self.observed_numpy = np.asarray(obs, dtype=np.float32)
+        self.background_rms_value = float(background_rms)
+        self.exp_time_value = float(exp_time)
+        err = np.sqrt(np.float32(background_rms) ** 2 +
+                      np.clip(self.observed_numpy, 0, np.inf) / np.float32(exp_time)).astype(np.float32)
+        self.err_numpy = err
+        self.observed_image = torch.as_tensor(self.observed_numpy)
+        self.err_map = torch.as_tensor(err)
+        self.fldj_of_x = fldj_of_x
+        example = prior.sample(seed=0)
+        self.pack_bij = dist.Pack(example)
+        self.unconstraining_bij = prior.experimental_default_event_space_bijector()
+        self.bij = dist.Chain([self.unconstraining_bij, self.pack_bij])
+
+    def log_prob(self, simulator, z):
+        z = torch.as_tensor(z)
+        if z.device.type != "cuda":
+            z = z.to(torch.device("cuda", torch.cuda.current_device()))
+        if z.dim() == 1:
+            z = z[None]
+        plan = simulator.lstsq_plan(self.observed_numpy, self.err_numpy, key=("backward", id(self)))
+        x = self.bij.forward(z)
+        xflat = torch.stack([v.reshape(-1) for v in dist.flatten(x)], dim=1).to(torch.float32)
+        logL, chi2 = _LstsqLogL.apply(xflat, simulator, plan)
+        at = x if self.fldj_of_x else self.pack_bij.forward(z)
+        log_prior = self.prior.log_prob(x) + self.unconstraining_bij.forward_log_det_jacobian(at)
+        return logL + log_prior, chi2

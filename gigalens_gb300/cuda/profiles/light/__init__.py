@@ -1,1 +1,1 @@
-from . import sersic  # noqa: F401
+from . import sersic, shapelets  # noqa: F401

@@ -5,8 +5,10 @@ supersample binning in one launch, ``gl_forward``).  The coordinate grid,
 PSF sub-kernels and observed data live in a device plan built once per
 simulator (and once per probabilistic model attached to it).
 """
+import ctypes
 from typing import Dict
 
+import numpy as np
 import torch
 
 from .. import _native as N
@@ -63,6 +65,52 @@ class LensSimulator(_sim.LensSimulatorInterface):
         N.call("gl_forward", plan.handle, N.ptr(x), None, bs, None, None, N.ptr(img), None, N.stream_ptr())
         return img.reshape(bs, self.numPix, self.numPix)
 
+    # least squares -----------------------------------------------------
+    def lstsq_plan(self, observed_image, err_map, prior=None, key=None) -> Plan:
+        """Plan of the linear-amplitude path for this observation and noise map."""
+        obs = observed_image.detach().cpu().numpy() if torch.is_tensor(observed_image) else observed_image
+        err = err_map.detach().cpu().numpy() if torch.is_tensor(err_map) else err_map
+        k = key if key is not None else (id(observed_image), id(err_map))
+        hit = self._lstsq_plans.get(k) if hasattr(self, "_lstsq_plans") else None
+        if hit is not None and hit[1] is observed_image and hit[2] is err_map:
+            return hit[0]
+        if not hasattr(self, "_lstsq_plans"):
+            self._lstsq_plans = {}
+        p = Plan(self.layout, [dict(sim_config=self.sim_config, observed=np.asarray(obs, np.float32),
+                                    err_map=None if err is None else np.asarray(err, np.float32))],
+                 prior=prior)
+        self._lstsq_plans[k] = (p, observed_image, err_map)
+        return p
+
+    def run_lstsq(self, plan: Plan, x: torch.Tensor, want_image=True, want_loglik=False):
+        """Run the least-squares kernels on flat physical parameters ``x``."""
+        x = x.to(torch.float32).contiguous()
+        bs = x.shape[0]
+        nbytes = ctypes.c_size_t(0)
+        D = ctypes.c_int(0)
+        N.call("gl_lstsq_workspace", plan.handle, bs, ctypes.byref(nbytes), ctypes.byref(D))
+        work = torch.empty(max(int(nbytes.value), 1), dtype=torch.uint8, device=x.device)
+        coeffs = torch.empty((bs, D.value), dtype=torch.float32, device=x.device)
+        img = torch.empty((bs, plan.max_pix), dtype=torch.float32, device=x.device) if want_image else None
+        logL = torch.empty(bs, dtype=torch.float32, device=x.device) if want_loglik else None
+        chi2 = torch.empty(bs, dtype=torch.float32, device=x.device) if want_loglik else None
+        N.call("gl_lstsq", plan.handle, N.ptr(x), None, bs, N.ptr(work), nbytes.value, N.ptr(coeffs), N.ptr(img),
+               N.ptr(logL), N.ptr(chi2), N.stream_ptr())
+        return dict(coeffs=coeffs, img=img, logL=logL, chi2=chi2, work=work, D=D.value)
+
     def lstsq_simulate(self, params, observed_image, err_map, return_stacked=False, return_coeffs=False,
                        no_deflection=False):
-        raise NotImplementedError("lstsq_simulate is provided by the least-squares kernels")
+        """``tf/simulator.py:99-165``: images with the linear amplitudes solved by
+        weighted least squares (pinv, rcond 1e-6)."""
+        if no_deflection:
+            raise NotImplementedError("no_deflection is not supported")
+        plan = self.lstsq_plan(observed_image, err_map)
+        x = self.layout.flatten_params(params)
+        r = self.run_lstsq(plan, x, want_image=not (return_stacked or return_coeffs))
+        bs, n = x.shape[0], self.numPix
+        if return_stacked:
+            X = r["work"][: bs * r["D"] * plan.max_pix * 4].view(torch.float32)
+            return X.reshape(bs, r["D"], n, n).permute(0, 2, 3, 1).squeeze()
+        if return_coeffs:
+            return r["coeffs"]
+        return r["img"].reshape(bs, n, n).squeeze()

@@ -25,6 +25,7 @@
 #ifndef GIGALENS_CUDA_H
 #define GIGALENS_CUDA_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -96,6 +97,9 @@ typedef struct {
   const float* observed;           /* host, N*N (may be NULL for simulate-only) */
   float background_rms;
   float exp_time;
+  const float* err_map;            /* host, N*N noise sigma for the least-squares
+                                      path; NULL = sqrt(bg^2 + clip(obs,0)/t),
+                                      the BackwardProbModel map (tf/model.py:92-94) */
 } gl_image_desc;
 
 /* Prior leaf: a distribution and its default event-space bijector, one per
@@ -173,9 +177,30 @@ int gl_bijector_forward(const gl_plan* plan, const float* z, int bs, float* x, v
  * (tf/profiles/mass/*.py deriv, tf/profiles/light/sersic.py light.)        */
 int gl_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,
                     const int* n_terms, float* out0, float* out1, void* stream);
+/* Shapelets.light (tf/profiles/light/shapelets.py:53-85, interpolate=False):
+ * params [3, n] = (beta, center_x, center_y) per point.  amps [D, n] with
+ * D = (n_max+1)(n_max+2)/2 gives out [n] = sum_k amps_k basis_k; amps NULL
+ * gives the unit-amplitude basis stack out [D, n] (use_lstsq).             */
+int gl_shapelets_eval(int n_max, const float* x, const float* y, int64_t n, const float* params,
+                      const float* amps, float* out, void* stream);
 /* tf/profiles/mass/epl.py:41,51-56: K = min(cap, #{i=1,2,..: i < log(1e-12)/log(max f)+2})
  * over n ellipticity pairs; writes the int K to *k_out (device).           */
 int gl_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out, void* stream);
+
+/* ---- linear amplitudes (least squares) -------------------------------- */
+/* LensSimulator.lstsq_simulate (tf/simulator.py:99-165) for a plan whose
+ * light profiles all have use_lstsq (unit-amplitude Sersic, Shapelets with
+ * interpolate=False): basis stack -> PSF + binning -> weighted normal
+ * equations G = X^T W^2 X, h = X^T W^2 y (W = 1/err_map) -> coeffs =
+ * pinv(G, rcond=1e-6) h -> img = sum_c coeffs_c X_c (no conversion factor,
+ * as the reference) -> BackwardProbModel likelihood with the error map
+ * (tf/model.py:157-163).  work: caller-allocated device scratch of
+ * gl_lstsq_workspace() bytes.  coeffs [bs, D] is required; img_out
+ * [bs, max_N^2], logL [bs], chi2 [bs] may be NULL.                        */
+int gl_lstsq_workspace(const gl_plan* plan, int bs, size_t* bytes, int* n_channels);
+int gl_lstsq(const gl_plan* plan, const float* x, const int* img_id, int bs, void* work,
+             size_t work_bytes, float* coeffs, float* img_out, float* logL, float* chi2,
+             void* stream);
 
 /* ---- optimizer step (graph-capturable) ------------------------------- */
 /* Keras Adam as used by ModellingSequence.MAP (tf/inference.py:34,
