@@ -146,6 +146,7 @@ SIGNATURES = [
     ("gl_shapelets_eval", _i, [_i, _vp, _vp, _i64, _vp, _vp, _vp, _vp]),
     ("gl_lstsq_workspace", _i, [_vp, _i, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_i)]),
     ("gl_lstsq", _i, [_vp, _vp, _vp, _i, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp]),
+    ("gl_lstsq_noalloc", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
 ]
 
 _lock = threading.Lock()

@@ -18,6 +18,7 @@
 //                  error map and chi^2 (BackwardProbModel, tf/model.py:157-163)
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "gl_corr.cuh"
@@ -751,4 +752,75 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   return GL_OK;
 }
 
+// ------------------------------------------------------------------ allocation-free variant
+// Fixed scratch for gl_lstsq_noalloc: a file-scope device array that every GPU
+// loading this library holds until the process exits.  Its host-side name is
+// only a stand-in for the symbol; the device address comes from
+// cudaGetSymbolAddress, looked up once per device with that device current.
+constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;   // 64 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+static void* g_noalloc_addr[kNoAllocMaxDevices];
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch_address(int device, void** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) {
+    set_error("gl_lstsq_noalloc: device %d out of range", device);
+    return GL_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("gl_lstsq_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return GL_ERR_CUDA;
+    }
+    g_noalloc_addr[device] = p;
+  }
+  *out = g_noalloc_addr[device];
+  return GL_OK;
+}
+
 }  // namespace gl
+
+extern "C" int gl_lstsq_noalloc(const gl_plan* plan, const float* x, const int* img_id, int bs,
+                                float* coeffs, float* img_out, float* logL, float* chi2,
+                                void* stream) {
+  using namespace gl;
+  if (!plan || bs < 0 || (bs > 0 && (!x || !coeffs))) {
+    set_error("gl_lstsq_noalloc: null plan, input or coeffs, or negative batch");
+    return GL_ERR_INVALID;
+  }
+  if (!plan->lsq) {
+    set_error("the plan has no linear-amplitude light profiles");
+    return GL_ERR_INVALID;
+  }
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != plan->device) {
+    set_error("plan was created on device %d but device %d is current", plan->device, dev);
+    return GL_ERR_INVALID;
+  }
+  if (logL || chi2)
+    for (int i = 0; i < plan->n_images; ++i)
+      if (!plan->img[i].obs) {
+        set_error("image %d has no observed data", i);
+        return GL_ERR_INVALID;
+      }
+  const LsqPlan* L = (const LsqPlan*)plan->lsq;
+  const size_t need = lsq_workspace_bytes(L, bs);
+  if (need > kNoAllocScratchBytes) {
+    const size_t per = lsq_workspace_bytes(L, 1);
+    set_error("gl_lstsq_noalloc: %d chains need %zu bytes of scratch, more than its fixed %zu bytes "
+              "(at most %zu chains for this plan); split the batch or use gl_lstsq",
+              bs, need, kNoAllocScratchBytes, per ? kNoAllocScratchBytes / per : (size_t)0);
+    return GL_ERR_INVALID;
+  }
+  void* scratch = nullptr;
+  int rc = noalloc_scratch_address(dev, &scratch);
+  if (rc) return rc;
+  return lsq_run(plan, x, img_id, bs, (float*)scratch, kNoAllocScratchBytes, coeffs, img_out, logL,
+                 chi2, (cudaStream_t)stream);
+}

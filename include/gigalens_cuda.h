@@ -202,6 +202,25 @@ int gl_lstsq(const gl_plan* plan, const float* x, const int* img_id, int bs, voi
              size_t work_bytes, float* coeffs, float* img_out, float* logL, float* chi2,
              void* stream);
 
+/* Allocation-free variant of gl_lstsq (no counterpart in the reference).
+ * Some callers cannot call cudaMalloc: a host framework whose own allocator
+ * has already reserved the GPU's memory, a serving loop that must not pay the
+ * device-wide synchronisation of cudaMalloc/cudaFree, or a plug-in callback
+ * that is not allowed to allocate.  This entry point takes the same inputs
+ * and outputs as gl_lstsq but no workspace: its scratch is a fixed 64 MiB
+ * array inside the library, which every GPU that loads the library keeps
+ * until the process exits.  It allocates nothing itself.
+ *  - Batches whose gl_lstsq_workspace() exceeds 64 MiB are rejected with
+ *    GL_ERR_INVALID and a message giving the largest batch that fits.
+ *  - The first call on a device looks up the array's device address (with
+ *    that device current); make that first call before any stream capture.
+ *  - Every call shares the one array and it keeps the last call's contents;
+ *    each call writes every scratch element it reads, so nothing needs
+ *    clearing.  Calls that overlap on the GPU (other streams, other host
+ *    threads) race on the array: serialise them.                          */
+int gl_lstsq_noalloc(const gl_plan* plan, const float* x, const int* img_id, int bs,
+                     float* coeffs, float* img_out, float* logL, float* chi2, void* stream);
+
 /* ---- optimizer step (graph-capturable) ------------------------------- */
 /* Keras Adam as used by ModellingSequence.MAP (tf/inference.py:34,
  * optimizer.apply_gradients): with t = *step + 1 and lr = schedule(*step),
