@@ -147,6 +147,16 @@ SIGNATURES = [
     ("gl_lstsq_workspace", _i, [_vp, _i, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_i)]),
     ("gl_lstsq", _i, [_vp, _vp, _vp, _i, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp]),
     ("gl_lstsq_noalloc", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    ("gl_nn_gemm", _i, [_i, _i, _i, _i, _i, _i, ctypes.c_float, _vp, _i, ctypes.c_longlong, _vp, _i,
+                        ctypes.c_longlong, ctypes.c_float, _vp, _i, ctypes.c_longlong, _i, _i, _vp]),
+    ("gl_nn_im2col3x3", _i, [_vp, _i, _i, _i, _i, _i, _vp, _vp]),
+    ("gl_nn_col2im3x3", _i, [_vp, _i, _i, _i, _i, _i, _vp, _vp]),
+    ("gl_nn_permute01", _i, [_vp, _i, _i, _i, _vp, _vp]),
+    ("gl_nn_bias_act", _i, [_vp, _vp, _i, _i, _i, _i, _vp]),
+    ("gl_nn_bias_act_backward", _i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp]),
+    ("gl_nn_gauss_nll", _i, [_vp, _vp, _i, _i, _vp, _vp, _vp]),
+    ("gl_nn_transpose", _i, [_vp, _i, _i, _vp, _vp]),
+    ("gl_nn_cast_bf16", _i, [_vp, _vp, ctypes.c_longlong, _vp]),
 ]
 
 _lock = threading.Lock()

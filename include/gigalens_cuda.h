@@ -239,6 +239,39 @@ typedef struct {
 int gl_adam_step(float* var, float* m, float* v, const float* grad, int64_t n, float grad_scale,
                  const gl_adam_cfg* cfg, int* step, void* stream);
 
+/* ---- learned MAP initialiser (no reference counterpart) ----------------
+ * Building blocks of the CNN that proposes ModellingSequence.MAP's starting
+ * ensemble (the `start` hook, gigalens/inference.py:34-57); orchestrated by
+ * gigalens_gb300/cuda/initializer.py.  Row-major float32 unless noted.     */
+/* C[b] = alpha op(A[b]) op(B[b]) + beta C[b] for b < batch; op(A) M x K,
+ * op(B) K x N; trans* = operand stored transposed; a_bf16: A is bfloat16
+ * (weights stored in BF16), accumulation is float32.  ksplit > 1 splits K
+ * across CTAs and adds the partial products atomically (beta must be 0;
+ * C is cleared first).                                                    */
+int gl_nn_gemm(int transA, int transB, int a_bf16, int M, int N, int K, float alpha, const void* A,
+               int lda, long long strideA, const float* B, int ldb, long long strideB, float beta,
+               float* C, int ldc, long long strideC, int batch, int ksplit, void* stream);
+/* 3x3, padding 1, channel-major activations: col [C*9][B][Ho*Wo] from
+ * X [C][B][H][W]; Ho = (H-1)/stride + 1.                                  */
+int gl_nn_im2col3x3(const float* X, int B, int C, int H, int W, int stride, float* col, void* stream);
+/* adjoint of im2col: dX [C][B][H][W] from dcol [C*9][B][Ho*Wo].            */
+int gl_nn_col2im3x3(const float* dcol, int B, int C, int H, int W, int stride, float* dX, void* stream);
+/* dst [B][A][C] = src [A][B][C] with the first two axes swapped.           */
+int gl_nn_permute01(const float* src, int A, int B, int C, float* dst, void* stream);
+/* Y [B][C][P] += bias[c]; ReLU when relu.                                  */
+int gl_nn_bias_act(float* Y, const float* bias, int B, int C, int P, int relu, void* stream);
+/* dY *= (Y > 0) when relu; dbias[c] = sum over b, p of dY.                 */
+int gl_nn_bias_act_backward(float* dY, const float* Y, int B, int C, int P, int relu, float* dbias,
+                            void* stream);
+/* Gaussian negative log-likelihood head: out [2d][B] (means, log-sigma
+ * clamped to [-12, 12]), target [d][B]; loss [d][B] and dout [2d][B] =
+ * gradient of the mean loss (either may be NULL).                          */
+int gl_nn_gauss_nll(const float* out, const float* target, int B, int d, float* loss, float* dout,
+                    void* stream);
+int gl_nn_transpose(const float* src, int rows, int cols, float* dst, void* stream);
+/* dst (bfloat16) = round-to-nearest(src), n elements.                      */
+int gl_nn_cast_bf16(const float* src, void* dst, long long n, void* stream);
+
 /* ---- diagnostics (no reference counterpart) --------------------------- */
 /* FP32 FMA throughput probe: blocks_per_sm*SMs blocks of 256 threads run
  * 8 independent FMA chains for iters*16 steps; *flops receives the flop
