@@ -1,31 +1,40 @@
 """Benchmark: lik+grad evaluations per second at 4096 chains x 90x90 pixels.
 
-Workload (the reference's headline configuration for this path): 90x90 base
-pixels at 0.065"/px, supersampling 2, Gaussian PSF of FWHM 0.1" (21x21 at
-base scale; the supersampled 41x41 kernel is generated directly on the fine
-grid), EPL(50) + external shear, elliptical Sersic lens light and source;
-4096 chains drawn from the configuration's parameter distributions;
-observed image = one seeded truth draw + Poisson noise at 1000 s + Gaussian
-background 0.2.  A step is one evaluation of the log posterior and its
-gradient for all 4096 chains: ONE launch of the fused forward+adjoint kernel
-(``gl_log_prob`` with a gradient).
+Workload (the reference's headline configuration for this path,
+``gigalens_gb300.workloads.config1``): 90x90 base pixels at 0.065"/px,
+supersampling 2, Gaussian PSF of FWHM 0.1" (21x21 at base scale; the
+supersampled 41x41 kernel is generated directly on the fine grid), EPL(50) +
+external shear, elliptical Sersic lens light and source; 4096 chains drawn
+from the configuration's parameter distributions; observed image = one
+seeded truth draw + Poisson noise at 1000 s + Gaussian background 0.2.  A
+step is one evaluation of the log posterior and its gradient for all 4096
+chains: ONE launch of the fused forward+adjoint kernel (``gl_log_prob`` with
+a gradient).
 
   value  whole-job evals/s with inputs resident in HBM, timed with CUDA events
          on the launching stream; L2 is flushed (256 MiB write) between steps
   e2e    the same through the public API (``ForwardProbModel.log_prob`` +
-         autograd backward) with pinned host buffers: H2D of z, D2H of
-         logp, chi^2 and the gradient inside the timed region
-  roofline  algorithmic FP32 flop per eval (forward + adjoint, the
-         minimal strided PSF form) x chains / kernel time, against the FP32
-         FMA peak measured live by a probe kernel at the same clocks
+         autograd) with pinned host buffers: H2D of z, D2H of logp, chi^2 and
+         the gradient inside the timed region
+  roofline  algorithmic FP32 flop per eval (forward + adjoint, the minimal
+         strided PSF form) x chains / kernel time, against the FP32 FMA peak
+         measured live by a probe kernel at the same clocks
   cpu_baseline  the float32 PyTorch-CPU restatement (autograd) on a bounded
          sample of the same workload, all host threads
+  secondary  quick timings of the other rows: a graph-captured MAP step at
+         the same workload, one uneven-batch least-squares launch (2048 x
+         100^2 px + 512 x 60^2 px, shapelets n_max = 8), one fixed-length HMC
+         iteration (2048 chains, 8 leapfrog steps)
 
 ``--impl reference`` times the reference's CPU path; TensorFlow is not
 installed, so that is the same float32 CPU restatement of the reference's
 algorithm (``kind: port``), on all host threads.
+``--time-to-map`` adds a second JSON line: the learned-initialiser
+measurement (train on simulated pairs, then time-to-chi^2/dof <= 1.05 for
+MAP from learned vs prior initialisation; minutes of GPU time).
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -43,64 +52,10 @@ if ROOT not in sys.path:
 
 METRIC = "lik+grad evals/s @4096x90^2px"
 UNIT = "evals/s"
-N_PIX, SS, DELTA, FWHM, PSF_BASE = 90, 2, 0.065, 0.1, 21
-BG_RMS, EXP_TIME, NITER = 0.2, 1000.0, 50
+N_PIX, SS, PSF_BASE = 90, 2, 21
 
 
-def workload_prior():
-    """A prior whose supports hold the configuration's distributions (the
-    bijectors of log_prob need one); chains are drawn from the configuration
-    itself by ``draw_chains``."""
-    from gigalens_gb300 import distributions as tfd
-
-    ie_ll = tfd.LogNormal(0.75 * math.log(10), 0.75 * math.log(10) / math.sqrt(3))
-    ie_src = tfd.LogNormal(1.25 * math.log(10), 0.75 * math.log(10) / math.sqrt(3))
-    return tfd.JointDistributionSequential([
-        tfd.JointDistributionSequential([
-            tfd.JointDistributionNamed(dict(theta_E=tfd.Uniform(1.0, 1.6), gamma=tfd.Uniform(1.8, 2.3),
-                                            e1=tfd.Normal(0, 0.1), e2=tfd.Normal(0, 0.1),
-                                            center_x=tfd.Normal(0, 0.05), center_y=tfd.Normal(0, 0.05))),
-            tfd.JointDistributionNamed(dict(gamma1=tfd.Normal(0, 0.05), gamma2=tfd.Normal(0, 0.05)))]),
-        tfd.JointDistributionSequential([tfd.JointDistributionNamed(dict(
-            R_sersic=tfd.Uniform(0.5, 1.5), n_sersic=tfd.Uniform(2, 6), e1=tfd.Normal(0, 0.1),
-            e2=tfd.Normal(0, 0.1), center_x=tfd.Normal(0, 0.05), center_y=tfd.Normal(0, 0.05), Ie=ie_ll))]),
-        tfd.JointDistributionSequential([tfd.JointDistributionNamed(dict(
-            R_sersic=tfd.Uniform(0.05, 0.4), n_sersic=tfd.Uniform(0.5, 4),
-            e1=tfd.TruncatedNormal(0, 0.15, -0.5, 0.5), e2=tfd.TruncatedNormal(0, 0.15, -0.5, 0.5),
-            center_x=tfd.Uniform(-0.3, 0.3), center_y=tfd.Uniform(-0.3, 0.3), Ie=ie_src))]),
-    ])
-
-
-def draw_chains(n, seed):
-    """Parameter structure of n chains from the configuration's distributions."""
-    import torch
-
-    r = np.random.default_rng(seed)
-    f = lambda a: torch.tensor(np.asarray(a, dtype=np.float32))
-    lens = {"theta_E": f(r.uniform(1.0, 1.6, n)), "gamma": f(r.uniform(1.8, 2.3, n)),
-            "e1": f(r.normal(0, 0.1, n)), "e2": f(r.normal(0, 0.1, n)),
-            "center_x": f(r.normal(0, 0.05, n)), "center_y": f(r.normal(0, 0.05, n))}
-    sh = {"gamma1": f(r.normal(0, 0.05, n)), "gamma2": f(r.normal(0, 0.05, n))}
-    ll = {"R_sersic": f(r.uniform(0.5, 1.5, n)), "n_sersic": f(r.uniform(2, 6, n)),
-          "e1": f(r.normal(0, 0.1, n)), "e2": f(r.normal(0, 0.1, n)),
-          "center_x": f(r.normal(0, 0.05, n)), "center_y": f(r.normal(0, 0.05, n)),
-          "Ie": f(10 ** r.uniform(0, 1.5, n))}
-    src = {"R_sersic": f(r.uniform(0.05, 0.4, n)), "n_sersic": f(r.uniform(0.5, 4, n)),
-           "e1": f(np.clip(r.normal(0, 0.15, n), -0.49, 0.49)), "e2": f(np.clip(r.normal(0, 0.15, n), -0.49, 0.49)),
-           "center_x": f(r.uniform(-0.3, 0.3, n)), "center_y": f(r.uniform(-0.3, 0.3, n)),
-           "Ie": f(10 ** r.uniform(0.5, 2, n))}
-    return [[lens, sh], [ll], [src]]
-
-
-def gaussian_psf(fwhm, pixel, side):
-    sigma = fwhm / (2.0 * math.sqrt(2.0 * math.log(2.0)))
-    r = (np.arange(side) - (side - 1) / 2.0) * pixel
-    g = np.exp(-0.5 * (r / sigma) ** 2)
-    k = np.outer(g, g)
-    return (k / k.sum()).astype(np.float32)
-
-
-def epl_terms(e1, e2, cap=NITER):
+def epl_terms(e1, e2, cap=50):
     """The reference's term-count rule (tf/profiles/mass/epl.py:41), float32."""
     e1 = np.asarray(e1, np.float32)
     e2 = np.asarray(e2, np.float32)
@@ -124,9 +79,7 @@ def flops_per_eval(K, n=N_PIX, ss=SS, k=2 * PSF_BASE - 1):
     Fpx = 84 + 10 * K
     Fpsf = 2 * P * (k + ss - 1) ** 2
     Flik = 12 * P
-    fwd = Ps * Fpx + Fpsf + Flik
-    adj = 2 * Ps * Fpx + Fpsf + Flik
-    return fwd, adj
+    return Ps * Fpx + Fpsf + Flik, 2 * Ps * Fpx + Fpsf + Flik
 
 
 class ClockSampler:
@@ -178,29 +131,33 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def make_observed_np(im_truth, exp_time, bg):
+    rng = np.random.default_rng(1)
+    counts = rng.poisson(np.clip(im_truth, 0, None) * exp_time) / exp_time
+    return (counts + rng.normal(scale=bg, size=im_truth.shape)).astype(np.float32)
+
+
 def cpu_port_rate(n_chains, seconds_hint=None):
     """Float32 PyTorch-CPU restatement (oracle) of lik+grad on n chains."""
     import torch
 
     from oracle import lens_oracle as O
-    from gigalens_gb300 import distributions as tfd
+    from gigalens_gb300 import workloads as W
 
     torch.set_num_threads(os.cpu_count() or 1)
-    model = dict(lenses=[("EPL", {"niter": NITER}), ("SHEAR", {})], lens_light=[("SERSIC_ELLIPSE", {})],
+    model = dict(lenses=[("EPL", {"niter": W.NITER}), ("SHEAR", {})], lens_light=[("SERSIC_ELLIPSE", {})],
                  source_light=[("SERSIC_ELLIPSE", {})])
-    ksub = gaussian_psf(FWHM, DELTA / SS, 2 * PSF_BASE - 1)
-    cfg = O.SimConfig(DELTA, N_PIX, SS, ksub.astype(np.float32))
-    xs = draw_chains(n_chains, seed=1)
-    truth = draw_chains(1, seed=0)
+    ksub = W.gaussian_psf(W.FWHM, W.DELTA_PIX / SS, 2 * PSF_BASE - 1)
+    cfg = O.SimConfig(W.DELTA_PIX, N_PIX, SS, ksub.astype(np.float32))
+    truth = W.draw_params(1, seed=0)
     im = O.simulate(model, cfg, [[{k: v.double() for k, v in d.items()} for d in g] for g in truth])[0].numpy()
-    obs = make_observed(im)
-    x = torch.stack([v.reshape(-1) for v in tfd.flatten(xs)], dim=1).float()
+    obs = make_observed_np(im, W.EXP_TIME, W.BG_RMS)
+    x = W.flat(W.draw_params(n_chains, seed=1)).float()
     K = epl_terms(x[:, 2].numpy(), x[:, 3].numpy())
 
     def once():
         xx = x.clone().requires_grad_(True)
-        ll, chi2 = O.forward_log_likelihood_flat(model, cfg, xx, obs.astype(np.float32), BG_RMS, EXP_TIME,
-                                                 dtype=torch.float32)
+        ll, _ = O.forward_log_likelihood_flat(model, cfg, xx, obs, W.BG_RMS, W.EXP_TIME, dtype=torch.float32)
         ll.sum().backward()
         return xx.grad
 
@@ -217,17 +174,9 @@ def cpu_port_rate(n_chains, seconds_hint=None):
     return n_chains * reps / el, torch.get_num_threads(), reps, el, K
 
 
-def make_observed(im_truth):
-    rng = np.random.default_rng(1)
-    counts = rng.poisson(np.clip(im_truth, 0, None) * EXP_TIME) / EXP_TIME
-    return (counts + rng.normal(scale=BG_RMS, size=im_truth.shape)).astype(np.float32)
-
-
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
 
 
 def run_reference(args):
@@ -235,8 +184,7 @@ def run_reference(args):
     if rank != 0:
         return
     n = args.ref_chains
-    rates = []
-    K = None
+    rates, K, cores = [], None, None
     for i in range(args.warmup + args.steps):
         r, cores, reps, el, K = cpu_port_rate(n, seconds_hint=args.ref_seconds)
         if i >= args.warmup:
@@ -256,6 +204,109 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _events(torch, n):
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
+def secondary_timings(torch, dev, pm, plan, z):
+    """Quick timings of MAP, least squares and HMC at their configurations."""
+    from gigalens_gb300 import _native as N
+    from gigalens_gb300 import distributions as tfd
+    from gigalens_gb300.model import PhysicalModel
+    from gigalens_gb300.simulator import SimulatorConfig
+    from gigalens_gb300 import workloads as W
+    from gigalens_gb300.cuda._plan import ModelLayout, Plan
+    from gigalens_gb300.cuda.model import log_prob_and_grad
+    from gigalens_gb300.cuda.optimizers import Adam, AdamState
+    from gigalens_gb300.cuda.profiles.light import shapelets
+    from gigalens_gb300.cuda.profiles.mass import epl, shear
+
+    out = {}
+    # MAP step (fused kernel + Adam), CUDA graph, 4096 x 90^2
+    bs = z.shape[0]
+    trial = z.clone()
+    logp, chi2, grad = torch.empty(bs, device=dev), torch.empty(bs, device=dev), torch.empty_like(z)
+    st = AdamState(trial, Adam(5e-3))
+
+    def step():
+        log_prob_and_grad(plan, trial, logp, chi2, grad)
+        st.apply(grad, -1.0 / (bs * N_PIX * N_PIX))
+
+    step()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            step()
+    torch.cuda.current_stream().wait_stream(s)
+    for _ in range(3):
+        g.replay()
+    e0, e1 = _events(torch, 2)
+    e0.record()
+    for _ in range(20):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    out["map_step_ms_4096x90px"] = e0.elapsed_time(e1) / 20
+    out["map_350_steps_s_4096x90px"] = out["map_step_ms_4096x90px"] * 350 / 1e3
+
+    # least squares, uneven batch: 2048 x 100^2 + 512 x 60^2, shapelets n_max = 8
+    phys = PhysicalModel([epl.EPL(50), shear.Shear()], [], [shapelets.Shapelets(8, use_lstsq=True, interpolate=False)])
+    lay = ModelLayout(phys)
+    ims = []
+    for n in (100, 60):
+        cfg = SimulatorConfig(delta_pix=W.DELTA_PIX, num_pix=n, supersample=2,
+                              kernel_supersampled=W.gaussian_psf(W.FWHM, W.DELTA_PIX / 2, 21))
+        o = np.random.default_rng(n).normal(scale=0.1, size=(n, n)).astype(np.float32) + 0.5
+        ims.append(dict(sim_config=cfg, observed=o, background_rms=0.1, exp_time=200.0))
+    lplan = Plan(lay, ims)
+    r = np.random.default_rng(3)
+    nb = 2560
+    cols = {"beta": r.uniform(0.05, 0.2, nb), "center_x": r.normal(0, 0.05, nb), "center_y": r.normal(0, 0.05, nb)}
+    lens = W.draw_params(nb, seed=4)[0]
+    xs = [[lens[0], lens[1]], [{k: torch.tensor(v, dtype=torch.float32) for k, v in cols.items()}]]
+    x = lay.flatten_params(xs)
+    img_id = torch.cat([torch.zeros(2048, dtype=torch.int32), torch.ones(512, dtype=torch.int32)]).to(dev)
+    wb, D = ctypes.c_size_t(0), ctypes.c_int(0)
+    N.call("gl_lstsq_workspace", lplan.handle, nb, ctypes.byref(wb), ctypes.byref(D))
+    work = torch.empty(wb.value, dtype=torch.uint8, device=dev)
+    co = torch.empty(nb, D.value, device=dev)
+    lg = torch.empty(nb, device=dev)
+
+    def lsq():
+        N.call("gl_lstsq", lplan.handle, N.ptr(x), N.ptr(img_id), nb, N.ptr(work), wb.value, N.ptr(co), None,
+               N.ptr(lg), None, N.stream_ptr())
+
+    lsq()
+    e0, e1 = _events(torch, 2)
+    e0.record()
+    lsq()
+    lsq()
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 2
+    out["lstsq_ms_2048x100px_plus_512x60px"] = t
+    out["lstsq_evals_per_s"] = nb / (t * 1e-3)
+    out["lstsq_workspace_gb"] = wb.value / 1e9
+    del work
+
+    # one fixed-length HMC iteration: 2048 chains x 8 leapfrog launches
+    zc = z[:2048].contiguous()
+    lp2, c22, g2 = torch.empty(2048, device=dev), torch.empty(2048, device=dev), torch.empty_like(zc)
+    log_prob_and_grad(plan, zc, lp2, c22, g2)
+    e0, e1 = _events(torch, 2)
+    e0.record()
+    for _ in range(8):
+        zc.add_(1e-4 * g2)
+        log_prob_and_grad(plan, zc, lp2, c22, g2)
+    e1.record()
+    torch.cuda.synchronize()
+    out["hmc_iteration_ms_2048x90px_L8"] = e0.elapsed_time(e1)
+    out["hmc_1500_iterations_s_2048x90px_L8"] = out["hmc_iteration_ms_2048x90px_L8"] * 1500 / 1e3
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as tdist
@@ -267,27 +318,21 @@ def run_ours(args):
     dev = torch.device("cuda", local)
 
     from gigalens_gb300 import _native as N
-    from gigalens_gb300 import distributions as tfd
-    from gigalens_gb300.model import PhysicalModel
-    from gigalens_gb300.simulator import SimulatorConfig
+    from gigalens_gb300 import workloads as W
     from gigalens_gb300.cuda.model import ForwardProbModel, log_prob_and_grad
-    from gigalens_gb300.cuda.profiles.light import sersic
-    from gigalens_gb300.cuda.profiles.mass import epl, shear
     from gigalens_gb300.cuda.simulator import LensSimulator
 
     bs = args.chains
-    phys = PhysicalModel([epl.EPL(NITER), shear.Shear()], [sersic.SersicEllipse()], [sersic.SersicEllipse()])
-    ksub = gaussian_psf(FWHM, DELTA / SS, 2 * PSF_BASE - 1)
-    cfg = SimulatorConfig(delta_pix=DELTA, num_pix=N_PIX, supersample=SS, kernel_supersampled=ksub)
+    phys = W.physical_model()
+    cfg = W.config1()
     truth_sim = LensSimulator(phys, cfg, bs=1)
-    truth = draw_chains(1, seed=0)
-    im = truth_sim.simulate(truth).cpu().numpy().astype(np.float64)
-    obs = make_observed(im)
-    prior = workload_prior()
-    pm = ForwardProbModel(prior, obs, background_rms=BG_RMS, exp_time=EXP_TIME)
+    im = truth_sim.simulate(W.draw_params(1, seed=0)).cpu().numpy().astype(np.float64)
+    obs = make_observed_np(im, W.EXP_TIME, W.BG_RMS)
+    prior = W.config_prior()
+    pm = ForwardProbModel(prior, obs, background_rms=W.BG_RMS, exp_time=W.EXP_TIME)
     sim = LensSimulator(phys, cfg, bs=bs)
     plan = sim.prob_plan(pm)
-    xs = draw_chains(bs, seed=1 + rank)
+    xs = W.draw_params(bs, seed=1 + rank)
     z = pm.bij.inverse(xs).to(torch.float32).to(dev).contiguous()
     K = epl_terms(xs[0][0]["e1"].numpy(), xs[0][0]["e2"].numpy())
     logp = torch.empty(bs, device=dev)
@@ -305,8 +350,7 @@ def run_ours(args):
     finite = bool(torch.isfinite(logp).all()) and bool(torch.isfinite(grad).all())
 
     # ---- device-resident timing: one fused launch per step, L2 flushed between
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    starts, ends = _events(torch, args.steps), _events(torch, args.steps)
     clocks = ClockSampler(local)
     if ws > 1:
         tdist.barrier()
@@ -333,10 +377,10 @@ def run_ours(args):
 
     # ---- FP32 peak (probe kernel, same clocks)
     probe_out = torch.empty(4096, device=dev)
-    flops = ctypes_double()
+    flops = ctypes.c_double(0.0)
     for _ in range(2):
         N.call("gl_probe_fp32_fma", N.ptr(probe_out), 2000, 4, flops, N.stream_ptr())
-    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pe0, pe1 = _events(torch, 2)
     pe0.record(stream)
     N.call("gl_probe_fp32_fma", N.ptr(probe_out), 2000, 4, flops, N.stream_ptr())
     pe1.record(stream)
@@ -350,14 +394,13 @@ def run_ours(args):
     e2e_times = []
     for i in range(args.warmup + args.steps):
         flush.fill_(float(i))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0, e1 = _events(torch, 2)
         e0.record(stream)
         z_dev.copy_(z_host, non_blocking=True)
         zz = z_dev.requires_grad_(True)
         lp, c2 = pm.log_prob(sim, zz)
         (gz,) = torch.autograd.grad(lp.sum(), zz)
-        dev_out = torch.cat([lp[:, None], c2[:, None], gz], dim=1)
-        out_host.copy_(dev_out, non_blocking=True)
+        out_host.copy_(torch.cat([lp[:, None], c2[:, None], gz], dim=1), non_blocking=True)
         e1.record(stream)
         torch.cuda.synchronize()
         z_dev = z_dev.detach()
@@ -372,6 +415,11 @@ def run_ours(args):
 
     fwd, adj = flops_per_eval(K)
     achieved = (fwd + adj) * bs / (t_step * 1e-3) / 1e12
+
+    secondary = None
+    if rank == 0 and not args.no_secondary:
+        del flush
+        secondary = secondary_timings(torch, dev, pm, plan, z)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -393,22 +441,22 @@ def run_ours(args):
                         "d2h_bytes_per_step": int(out_host.numel() * 4),
                         "api": "ForwardProbModel.log_prob + torch.autograd.grad, pinned host buffers"},
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                             "frac": achieved / fp32_peak, "traffic": None,
+                             "frac": achieved / fp32_peak, "traffic": args.traffic_per_launch,
                              "flop_per_eval": fwd + adj,
                              "peak_source": "FP32 FMA probe kernel measured in this run (MEASURED_PEAKS.json "
                                             "holds no FP32 figure)"},
                 "cpu_baseline": cpu,
                 "gpu_launches": args.steps,
-                "clocks": clk}
+                "clocks": clk,
+                "secondary": secondary}
         print(json.dumps(line), flush=True)
+        if args.time_to_map:
+            from gigalens_gb300.cuda import initializer
+
+            initializer.main(["--pairs", str(args.ttm_pairs), "--epochs", str(args.ttm_epochs),
+                              "--lenses", str(args.ttm_lenses)])
     if ws > 1:
         tdist.destroy_process_group()
-
-
-def ctypes_double():
-    import ctypes
-
-    return ctypes.c_double(0.0)
 
 
 def main():
@@ -423,6 +471,13 @@ def main():
     ap.add_argument("--ref-chains", type=int, default=8)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--traffic-per-launch", type=float, default=None,
+                    help="DRAM bytes per fused launch from an ncu capture (recorded in the JSON line)")
+    ap.add_argument("--time-to-map", action="store_true")
+    ap.add_argument("--ttm-pairs", type=int, default=2_000_000)
+    ap.add_argument("--ttm-epochs", type=int, default=20)
+    ap.add_argument("--ttm-lenses", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -286,14 +286,12 @@ __device__ void phase_pixels_forward(const FusedArgs& a, const DevImage& I, floa
   const int NN = I.N * I.N;
   const int total = I.nplanes * NN;
   const float2* grid = reinterpret_cast<const float2*>(I.grid);
-  for (int v = threadIdx.x; v < total; v += kThreads) {
+  // light of one pixel from its coordinates and deflection, stored to its plane
+  auto finish = [&](int v, float2 xy, float ax, float ay) {
     const int pq = v / NN;
     const int r = v - pq * NN;
     const int Y = r / I.N, X = r - Y * I.N;
     const int q = pq - (pq / I.ss) * I.ss;
-    const float2 xy = __ldg(grid + v);
-    float ax, ay;
-    epl_deflect(c.epl, st.tab, xy.x, xy.y, ax, ay);
     float bx = xy.x - ax, by = xy.y - ay;
     if (T::kShear) {
       bx = bx - (c.g1 * xy.x + c.g2 * xy.y);
@@ -304,6 +302,21 @@ __device__ void phase_pixels_forward(const FusedArgs& a, const DevImage& I, floa
     img += sersic_light(c.src, bx, by);
     if (isnan(img)) img = 0.f;
     sm[I.offI + pq * I.N * I.pitchI + Y * I.pitchI + I.padI[q] + X] = img;
+  };
+  // two pixels per iteration: their series evaluations interleave
+  int v = threadIdx.x;
+  for (; v + kThreads < total; v += 2 * kThreads) {
+    const float2 xy0 = __ldg(grid + v), xy1 = __ldg(grid + v + kThreads);
+    float ax0, ay0, ax1, ay1;
+    epl_deflect2(c.epl, st.tab, xy0.x, xy0.y, xy1.x, xy1.y, ax0, ay0, ax1, ay1);
+    finish(v, xy0, ax0, ay0);
+    finish(v + kThreads, xy1, ax1, ay1);
+  }
+  if (v < total) {
+    const float2 xy = __ldg(grid + v);
+    float ax, ay;
+    epl_deflect(c.epl, st.tab, xy.x, xy.y, ax, ay);
+    finish(v, xy, ax, ay);
   }
 }
 
@@ -489,26 +502,12 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
       }
     }
     __syncthreads();
-    // EPL series table: p_n and s_n = sum_{m<=n} d ln|p_m|/dt (warp 0, scan)
+    // EPL series coefficient table (warp 0)
     const int K = st.K[im];
     if (tid < 32) {
       const int* e = a.epl.col;
       const float e1 = pget(st.x, e[2], 0.f), e2 = pget(st.x, e[3], 0.f);
-      const float f = epl_f_of(e1, e2);
-      const float t = pget(st.x, e[1], 2.f) - 1.f;
-      float carry = 0.f;
-      for (int base = 1; base <= K; base += 32) {
-        const int n = base + tid;
-        float dl = (n <= K) ? epl_dlnp_dt(t, n) : 0.f;
-        // inclusive scan over the warp
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          float y = __shfl_up_sync(0xffffffffu, dl, o);
-          if (tid >= o) dl += y;
-        }
-        if (n <= K) st.tab[n] = make_float2(epl_prefac(f, t, n), carry + dl);
-        carry += __shfl_sync(0xffffffffu, dl, 31);
-      }
+      epl_build_table(st.tab, epl_f_of(e1, e2), pget(st.x, e[1], 2.f) - 1.f, K, tid);
     }
     __syncthreads();
 

@@ -140,21 +140,9 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
     __syncthreads();
     const int K = st.K[im];
     const int* e = a.epl.col;
-    if (tid < 32) {
-      const float f = epl_f_of(lpget(st.x, e[2], 0.f), lpget(st.x, e[3], 0.f));
-      const float t = lpget(st.x, e[1], 2.f) - 1.f;
-      float carry = 0.f;
-      for (int base = 1; base <= K; base += 32) {
-        const int n = base + tid;
-        float dl = (n <= K) ? epl_dlnp_dt(t, n) : 0.f;
-        for (int o = 1; o < 32; o <<= 1) {
-          const float y = __shfl_up_sync(0xffffffffu, dl, o);
-          if (tid >= o) dl += y;
-        }
-        if (n <= K) st.tab[n] = make_float2(epl_prefac(f, t, n), carry + dl);
-        carry += __shfl_sync(0xffffffffu, dl, 31);
-      }
-    }
+    if (tid < 32)
+      epl_build_table(st.tab, epl_f_of(lpget(st.x, e[2], 0.f), lpget(st.x, e[3], 0.f)),
+                      lpget(st.x, e[1], 2.f) - 1.f, K, tid);
     __syncthreads();
     // ray-trace the band: beta per (plane, band row, column)
     {

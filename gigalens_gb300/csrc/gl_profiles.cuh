@@ -113,39 +113,66 @@ __device__ __forceinline__ EplGeom epl_geom(const EplC& c, float x, float y) {
   return g;
 }
 
-// Forward deflection.  tab[n] = (p_n, s_n), n = 1..K.
+// The series as a polynomial: last_n = A_n z^(2n+1) with z = e^{ia},
+// A_n = prod_{m<=n} p_m, so F = sum_{n<=K} last_n = z P(w), P(w) = sum A_n w^n,
+// w = z^2 = e^{2ia}.  tab[n] = (A_n, s_n A_n), n = 0..K (A_0 = 1, s_0 = 0);
+// P is evaluated by Horner's rule (4 FP32 operations per term).
+__device__ __forceinline__ void epl_series_F(const EplGeom& g, const float2* __restrict__ tab, int K,
+                                             float& Fx, float& Fy) {
+  float Px = tab[K].x, Py = 0.f;
+#pragma unroll 4
+  for (int n = K - 1; n >= 0; --n) {
+    const float a = tab[n].x;
+    const float nx = fmaf(Px, g.Cs2, fmaf(-Py, g.Ss2, a));
+    Py = fmaf(Px, g.Ss2, Py * g.Cs2);
+    Px = nx;
+  }
+  Fx = g.Cs * Px - g.Ss * Py;
+  Fy = g.Cs * Py + g.Ss * Px;
+}
+
+// Forward deflection.
 __device__ __forceinline__ void epl_deflect(const EplC& c, const float2* __restrict__ tab, float x,
                                             float y, float& ax, float& ay) {
   EplGeom g = epl_geom(c, x, y);
-  float lx = g.Cs, ly = g.Ss, Fx = g.Cs, Fy = g.Ss;
-  int n = 1;
-#pragma unroll 1
-  for (; n + 1 <= c.K; n += 2) {
-    float p0 = tab[n].x, p1 = tab[n + 1].x;
-    float u = p0 * lx, v = p0 * ly;
-    lx = fmaf(g.Cs2, u, -g.Ss2 * v);
-    ly = fmaf(g.Ss2, u, g.Cs2 * v);
-    Fx += lx;
-    Fy += ly;
-    u = p1 * lx;
-    v = p1 * ly;
-    lx = fmaf(g.Cs2, u, -g.Ss2 * v);
-    ly = fmaf(g.Ss2, u, g.Cs2 * v);
-    Fx += lx;
-    Fy += ly;
-  }
-  if (n <= c.K) {
-    float p0 = tab[n].x;
-    float u = p0 * lx, v = p0 * ly;
-    lx = fmaf(g.Cs2, u, -g.Ss2 * v);
-    ly = fmaf(g.Ss2, u, g.Cs2 * v);
-    Fx += lx;
-    Fy += ly;
-  }
+  float Fx, Fy;
+  epl_series_F(g, tab, c.K, Fx, Fy);
   float P = c.A * exp2f(c.tm1 * (c.log2b - g.l2Rc));
   float arx = Fx * P, ary = Fy * P;
   ax = arx * c.cph - ary * c.sph;
   ay = arx * c.sph + ary * c.cph;
+}
+
+// Two pixels at once (independent Horner chains interleave for ILP).
+__device__ __forceinline__ void epl_deflect2(const EplC& c, const float2* __restrict__ tab, float x0,
+                                             float y0, float x1, float y1, float& ax0, float& ay0,
+                                             float& ax1, float& ay1) {
+  const EplGeom g0 = epl_geom(c, x0, y0), g1 = epl_geom(c, x1, y1);
+  float P0x = tab[c.K].x, P0y = 0.f, P1x = P0x, P1y = 0.f;
+#pragma unroll 4
+  for (int n = c.K - 1; n >= 0; --n) {
+    const float a = tab[n].x;
+    const float n0 = fmaf(P0x, g0.Cs2, fmaf(-P0y, g0.Ss2, a));
+    const float n1 = fmaf(P1x, g1.Cs2, fmaf(-P1y, g1.Ss2, a));
+    P0y = fmaf(P0x, g0.Ss2, P0y * g0.Cs2);
+    P1y = fmaf(P1x, g1.Ss2, P1y * g1.Cs2);
+    P0x = n0;
+    P1x = n1;
+  }
+  {
+    const float Fx = g0.Cs * P0x - g0.Ss * P0y, Fy = g0.Cs * P0y + g0.Ss * P0x;
+    const float P = c.A * exp2f(c.tm1 * (c.log2b - g0.l2Rc));
+    const float arx = Fx * P, ary = Fy * P;
+    ax0 = arx * c.cph - ary * c.sph;
+    ay0 = arx * c.sph + ary * c.cph;
+  }
+  {
+    const float Fx = g1.Cs * P1x - g1.Ss * P1y, Fy = g1.Cs * P1y + g1.Ss * P1x;
+    const float P = c.A * exp2f(c.tm1 * (c.log2b - g1.l2Rc));
+    const float arx = Fx * P, ary = Fy * P;
+    ax1 = arx * c.cph - ary * c.sph;
+    ay1 = arx * c.sph + ary * c.cph;
+  }
 }
 
 struct EplAcc {
@@ -160,38 +187,68 @@ struct EplState {
   float Fx, Fy, Hx, Hy, Tx, Ty, P, ax, ay;
 };
 
+// F = z P(w), H = sum n last_n = z w P'(w), T = sum s_n last_n = z Q(w) with
+// Q(w) = sum s_n A_n w^n: Horner with derivative, three chains per term.
 __device__ __forceinline__ EplState epl_state(const EplC& c, const float2* __restrict__ tab, float x,
                                               float y) {
   EplState s;
   s.g = epl_geom(c, x, y);
-  float lx = s.g.Cs, ly = s.g.Ss, Fx = s.g.Cs, Fy = s.g.Ss;
-  float Hx = 0.f, Hy = 0.f, Tx = 0.f, Ty = 0.f;
-  float nf = 1.f;
+  const float wx = s.g.Cs2, wy = s.g.Ss2;
+  const float2 top = tab[c.K];
+  float Px = top.x, Py = 0.f, Dx = 0.f, Dy = 0.f, Qx = top.y, Qy = 0.f;
 #pragma unroll 2
-  for (int n = 1; n <= c.K; ++n) {
-    float2 ps = tab[n];
-    float u = ps.x * lx, v = ps.x * ly;
-    lx = fmaf(s.g.Cs2, u, -s.g.Ss2 * v);
-    ly = fmaf(s.g.Ss2, u, s.g.Cs2 * v);
-    Fx += lx;
-    Fy += ly;
-    Hx = fmaf(nf, lx, Hx);
-    Hy = fmaf(nf, ly, Hy);
-    Tx = fmaf(ps.y, lx, Tx);
-    Ty = fmaf(ps.y, ly, Ty);
-    nf += 1.f;
+  for (int n = c.K - 1; n >= 0; --n) {
+    const float2 ab = tab[n];
+    // D <- D w + P (derivative), then P <- P w + A_n, Q <- Q w + B_n
+    const float dx = fmaf(Dx, wx, fmaf(-Dy, wy, Px));
+    Dy = fmaf(Dx, wy, fmaf(Dy, wx, Py));
+    Dx = dx;
+    const float px = fmaf(Px, wx, fmaf(-Py, wy, ab.x));
+    Py = fmaf(Px, wy, Py * wx);
+    Px = px;
+    const float qx = fmaf(Qx, wx, fmaf(-Qy, wy, ab.y));
+    Qy = fmaf(Qx, wy, Qy * wx);
+    Qx = qx;
   }
-  s.Fx = Fx;
-  s.Fy = Fy;
-  s.Hx = Hx;
-  s.Hy = Hy;
-  s.Tx = Tx;
-  s.Ty = Ty;
+  const float zx = s.g.Cs, zy = s.g.Ss;
+  s.Fx = zx * Px - zy * Py;
+  s.Fy = zx * Py + zy * Px;
+  const float zwx = zx * wx - zy * wy, zwy = zx * wy + zy * wx;   // z w = z^3
+  s.Hx = zwx * Dx - zwy * Dy;
+  s.Hy = zwx * Dy + zwy * Dx;
+  s.Tx = zx * Qx - zy * Qy;
+  s.Ty = zx * Qy + zy * Qx;
   s.P = c.A * exp2f(c.tm1 * (c.log2b - s.g.l2Rc));
-  float arx = Fx * s.P, ary = Fy * s.P;
+  float arx = s.Fx * s.P, ary = s.Fy * s.P;
   s.ax = arx * c.cph - ary * c.sph;
   s.ay = arx * c.sph + ary * c.cph;
   return s;
+}
+
+// Per-chain series table, built by one warp: tab[n] = (A_n, s_n A_n), n = 0..K,
+// with A_n = prod_{m<=n} p_m (p_m with the reference's op order) and
+// s_n = sum_{m<=n} d ln|p_m| / dt, both as warp scans.
+__device__ __forceinline__ void epl_build_table(float2* tab, float f, float t, int K, int lane) {
+  float carry_p = 1.f, carry_s = 0.f;
+  for (int base = 0; base <= K; base += 32) {
+    const int n = base + lane;
+    const bool term = n >= 1 && n <= K;
+    float p = term ? epl_prefac(f, t, n) : 1.f;
+    float dl = term ? epl_dlnp_dt(t, n) : 0.f;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float yp = __shfl_up_sync(0xffffffffu, p, o);
+      const float yd = __shfl_up_sync(0xffffffffu, dl, o);
+      if (lane >= o) {
+        p *= yp;
+        dl += yd;
+      }
+    }
+    const float A = carry_p * p, S = carry_s + dl;
+    if (n <= K) tab[n] = make_float2(A, S * A);
+    carry_p *= __shfl_sync(0xffffffffu, p, 31);
+    carry_s += __shfl_sync(0xffffffffu, dl, 31);
+  }
 }
 
 // Accumulate the contribution of the deflection adjoint (abx, aby).

@@ -44,7 +44,13 @@ def _cuda_dev():
 class ModellingSequence(_inf.ModellingSequenceInterface):
     map_chi2_history = None
 
-    def MAP(self, optimizer: Adam = None, start=None, n_samples=500, num_steps=350, seed=0, use_graph=True):
+    def MAP(self, optimizer: Adam = None, start=None, n_samples=500, num_steps=350, seed=0, use_graph=True,
+            stop_chi2=None, check_every=25):
+        """Multi-start Adam; returns the unconstrained parameters of all chains.
+
+        ``stop_chi2``: stop early once the best chain's chi^2 is <= this value
+        (checked every ``check_every`` steps; ``map_steps_run`` records the
+        steps taken)."""
         optimizer = optimizer if optimizer is not None else Adam(1e-3)
         dev = _cuda_dev()
         prior = self.prob_model.prior
@@ -68,23 +74,41 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
             hist.index_copy_(0, idx, torch.nan_to_num(chi2, nan=float("inf")).amin().reshape(1))
             state.apply(grad, scale)
 
+        self.map_steps_run = 0
         if num_steps <= 0:
             return trial
+
+        def reached(done):
+            return stop_chi2 is not None and float(hist[:done].min()) <= stop_chi2
+
         if not use_graph:
-            for _ in range(num_steps):
+            for i in range(num_steps):
                 step()
+                if (i + 1) % check_every == 0 and reached(i + 1):
+                    self.map_steps_run = i + 1
+                    break
+            else:
+                self.map_steps_run = num_steps
         else:
             # one eager step outside capture (allocator warm-up), then capture one step
             step()
-            s = torch.cuda.Stream()
-            s.wait_stream(torch.cuda.current_stream())
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.stream(s):
-                with torch.cuda.graph(g, stream=s):
-                    step()
-            torch.cuda.current_stream().wait_stream(s)
-            for _ in range(num_steps - 1):
-                g.replay()
+            done = 1
+            if not reached(done):
+                s = torch.cuda.Stream()
+                s.wait_stream(torch.cuda.current_stream())
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.stream(s):
+                    with torch.cuda.graph(g, stream=s):
+                        step()
+                torch.cuda.current_stream().wait_stream(s)
+                while done < num_steps:
+                    n = min(check_every if stop_chi2 is not None else num_steps, num_steps - done)
+                    for _ in range(n):
+                        g.replay()
+                    done += n
+                    if reached(done):
+                        break
+            self.map_steps_run = done
         self.map_chi2_history = hist
         self.map_chi2 = chi2
         self.map_log_prob = logp

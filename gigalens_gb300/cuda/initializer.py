@@ -324,18 +324,106 @@ class LearnedInitializer:
         return z.detach(), False
 
 
-def time_to_chi2(seq, start_z, optimizer_fn, num_steps, threshold=1.05, extra_seconds=0.0):
-    """Run MAP from ``start_z``; return (seconds to first step whose best chi^2
-    is <= threshold or None, per-step history, seconds per step)."""
+def _map_time(seq, start_z, lr, num_steps, threshold):
+    """Wall seconds for MAP from ``start_z`` to reach best chi^2 <= threshold
+    (None if not within num_steps), and the steps taken."""
+    from .optimizers import Adam
+
     z_struct = seq.prob_model.bij.forward(start_z)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    seq.MAP(optimizer_fn(), start=z_struct, n_samples=start_z.shape[0], num_steps=num_steps)
+    seq.MAP(Adam(lr), start=z_struct, n_samples=start_z.shape[0], num_steps=num_steps, stop_chi2=threshold,
+            check_every=10)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
-    hist = seq.map_chi2_history.detach().cpu()
-    per_step = el / max(num_steps, 1)
+    hist = seq.map_chi2_history[: seq.map_steps_run].detach().cpu()
     hit = (hist <= threshold).nonzero()
     if len(hit) == 0:
-        return None, hist, per_step
-    return extra_seconds + (int(hit[0]) + 1) * per_step, hist, per_step
+        return None, seq.map_steps_run, el
+    return el, int(hit[0]) + 1, el
+
+
+def evaluate_time_to_map(net, n_lenses=256, n_chains=4096, num_steps=350, lr=5e-3, threshold=1.05, seed=10_000):
+    """Time to chi^2/dof <= threshold (the reference's per-pixel mean chi^2,
+    tf/model.py:84-86) for MAP from prior draws and from the learned proposal,
+    on ``n_lenses`` unseen config-0 lenses.  The learned time includes the
+    network and the proposal's log-posterior evaluations."""
+    from .inference import ModellingSequence
+    from .model import ForwardProbModel
+    from .simulator import LensSimulator
+
+    prior = W.config_prior()
+    cfg = W.config0()
+    phys = W.physical_model()
+    sim1 = LensSimulator(phys, cfg, bs=1)
+    init = LearnedInitializer(net)
+    rows = []
+    for k in range(n_lenses):
+        truth = W.draw_params(1, seed=seed + k)
+        img = sim1.simulate_flat(W.flat(truth).to(net.dev))
+        obs = W.observe(img, seed=seed + k)[0].cpu().numpy()
+        pm = ForwardProbModel(prior, obs, background_rms=W.BG_RMS, exp_time=W.EXP_TIME)
+        seq = ModellingSequence(phys, pm, cfg)
+        sim = LensSimulator(phys, cfg, bs=n_chains)
+        prior_z = pm.bij.inverse(prior.sample(n_chains, seed=seed + 7 * k + 1)).to(net.dev, torch.float32)
+        t_prior, s_prior, _ = _map_time(seq, prior_z, lr, num_steps, threshold)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        z, fell_back = init.propose(obs, n_chains, pm, sim, seed=k, prior_z=prior_z)
+        torch.cuda.synchronize()
+        t_prop = time.perf_counter() - t0
+        t_learn, s_learn, _ = _map_time(seq, z, lr, num_steps, threshold)
+        rows.append(dict(lens=k, prior_s=t_prior, prior_steps=s_prior, learned_s=None if t_learn is None else
+                         t_learn + t_prop, learned_steps=s_learn, proposal_s=t_prop, fell_back=fell_back))
+    inf = float("inf")
+    tp = np.array([r["prior_s"] if r["prior_s"] is not None else inf for r in rows])
+    tl = np.array([r["learned_s"] if r["learned_s"] is not None else inf for r in rows])
+    summary = dict(n_lenses=n_lenses, n_chains=n_chains, max_steps=num_steps, lr=lr, threshold=threshold,
+                   prior_reached=float(np.isfinite(tp).mean()), learned_reached=float(np.isfinite(tl).mean()),
+                   prior_median_s=float(np.median(tp)), learned_median_s=float(np.median(tl)),
+                   fallbacks=int(sum(r["fell_back"] for r in rows)))
+    both = np.isfinite(tp) & np.isfinite(tl)
+    if both.any():
+        summary["median_ratio_learned_over_prior_where_both_reached"] = float(np.median(tl[both] / tp[both]))
+    return summary, rows
+
+
+def main(argv=None):
+    """Train the initialiser on simulated pairs and measure time-to-MAP, learned vs prior init."""
+    import argparse
+    import json
+
+    from .. import distributions as tfd
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--pairs", type=int, default=2_000_000)
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--batch", type=int, default=1024)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--lenses", type=int, default=256)
+    ap.add_argument("--chains", type=int, default=4096)
+    ap.add_argument("--steps", type=int, default=350)
+    ap.add_argument("--map-lr", type=float, default=5e-3)
+    args = ap.parse_args(argv)
+    torch.cuda.set_device(0)
+    prior = W.config_prior()
+    bij = tfd.Chain([prior.experimental_default_event_space_bijector(), tfd.Pack(prior.sample(seed=0))])
+    t0 = time.perf_counter()
+    imgs, zs = make_training_set(args.pairs, seed=1, prob_bijector=bij)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    net = LensCNN(d=22, seed=0)
+    t0 = time.perf_counter()
+    hist = train(net, imgs, zs, epochs=args.epochs, batch=args.batch, lr=args.lr)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del imgs, zs
+    summary, rows = evaluate_time_to_map(net, args.lenses, args.chains, args.steps, args.map_lr)
+    summary.update(pairs=args.pairs, epochs=args.epochs, datagen_s=t_data, train_s=t_train,
+                   train_steps=int(hist.numel()), final_loss=float(hist[-50:].mean()))
+    print(json.dumps({"metric": "time-to-MAP chi2/dof<=1.05, learned vs prior init", **summary}), flush=True)
+    return summary, rows
+
+
+if __name__ == "__main__":
+    main()
