@@ -404,6 +404,7 @@ def main(argv=None):
     ap.add_argument("--chains", type=int, default=4096)
     ap.add_argument("--steps", type=int, default=350)
     ap.add_argument("--map-lr", type=float, default=5e-3)
+    ap.add_argument("--out", default=None, help="write the summary and per-lens rows as JSON here")
     args = ap.parse_args(argv)
     torch.cuda.set_device(0)
     prior = W.config_prior()
@@ -422,6 +423,9 @@ def main(argv=None):
     summary.update(pairs=args.pairs, epochs=args.epochs, datagen_s=t_data, train_s=t_train,
                    train_steps=int(hist.numel()), final_loss=float(hist[-50:].mean()))
     print(json.dumps({"metric": "time-to-MAP chi2/dof<=1.05, learned vs prior init", **summary}), flush=True)
+    if args.out:
+        with open(args.out, "w") as fh:
+            json.dump(dict(summary=summary, rows=rows), fh, indent=1)
     return summary, rows
 
 
