@@ -1,6 +1,7 @@
 // Host side of the C ABI: plan construction (validation, PSF+binning
 // sub-kernels, coordinate grid, device constants) and the compute entry
 // points.  No compute happens here; every entry point enqueues kernels.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -185,10 +186,14 @@ static int build_image(const gl_image_desc& g, DevImage& I, HostImage& hi) {
           hi.kern[((p * ss + q) * KS + m) * I.ksp + l] = (float)val;
         }
   // shared-memory layout
-  I.ncb = ((N + kColBlock - 1) / kColBlock + 3) & ~3;
-  I.rows2 = (N + 1) & ~1;
-  const int segn = (kColBlock + KS - 1 + 3) & ~3;
-  int pitch = (int)align_up(kColBlock * (I.ncb - 1) + segn, 4);
+  // The pitch covers the segments read by the fused kernel (kFusedCB columns
+  // per unit) and by the least-squares kernel (kColBlock columns per unit).
+  I.ncb = ((N + kFusedCB - 1) / kFusedCB + 1) & ~1;
+  I.units = N * I.ncb;
+  const int seg_f = (kFusedCB + KS - 1 + 3) & ~3;
+  const int seg_l = (kColBlock + KS - 1 + 3) & ~3;
+  const int ncb_l = (N + kColBlock - 1) / kColBlock;
+  int pitch = (int)align_up(std::max(kFusedCB * (I.ncb - 1) + seg_f, kColBlock * (ncb_l - 1) + seg_l), 4);
   if ((pitch / 4) % 2 == 0) pitch += 4;
   for (int q = 0; q < ss; ++q) I.padI[q] = I.d[q];
   I.pitchI = pitch;
@@ -206,15 +211,18 @@ static int build_image(const gl_image_desc& g, DevImage& I, HostImage& hi) {
   const float lo = 0.f - (float)((double)(S - 1) / 2.0);
   const double ra0 = (double)(float)((float)((float)T[0] * lo) + (float)((float)T[1] * lo));
   const double dec0 = (double)(float)((float)((float)T[2] * lo) + (float)((float)T[3] * lo));
-  hi.grid.assign((size_t)I.nplanes * N * N * 2, 0.f);
+  hi.grid.assign((size_t)I.nplanes * N * N * 4, 0.f);
   for (int p = 0; p < ss; ++p)
     for (int q = 0; q < ss; ++q)
       for (int Y = 0; Y < N; ++Y)
         for (int X = 0; X < N; ++X) {
           const double row = ss * Y + p, col = ss * X + q;
-          const size_t v = (((size_t)(p * ss + q) * N + Y) * N + X) * 2;
+          const int pq = p * ss + q;
+          const size_t v = (((size_t)pq * N + Y) * N + X) * 4;
           hi.grid[v] = (float)(T[0] * col + T[1] * row + ra0);
           hi.grid[v + 1] = (float)(T[2] * col + T[3] * row + dec0);
+          const int off = I.offI + (pq * N + Y) * I.pitchI + I.padI[q] + X;
+          memcpy(&hi.grid[v + 2], &off, sizeof(int));
         }
   I.t00 = (float)T[0];
   I.t01 = (float)T[1];

@@ -1,8 +1,8 @@
 // Register-blocked 1-D correlation rows: the building block of the
 // PSF + supersample-binning correlations (forward and transposed) of the
 // fused and least-squares kernels.  A parity plane row segment and one
-// sub-kernel row are held in registers; each thread produces kColBlock
-// adjacent outputs.
+// sub-kernel row are held in registers; each thread produces CB adjacent
+// outputs (kFusedCB in the fused kernel, kColBlock in the least-squares one).
 #pragma once
 #include "gl_internal.cuh"
 
@@ -10,13 +10,14 @@ namespace gl {
 
 // ---------------------------------------------------------------- correlation
 // acc[c] += sum_l k[l] * seg[c + l]  (REV: k[KS-1-l]); seg and krow 16-byte aligned.
-template <int KS, bool REV>
+// The segment is held in registers; the kernel row is read four taps at a
+// time (a broadcast 16-byte load), which keeps the live set near CB + SEGN.
+template <int KS, bool REV, int CB = kColBlock>
 __device__ __forceinline__ void corr_row(const float* __restrict__ seg,
-                                         const float* __restrict__ krow, float (&acc)[kColBlock]) {
-  constexpr int SEGN = (kColBlock + KS - 1 + 3) & ~3;
-  constexpr int KSP = (KS + 3) & ~3;
+                                         const float* __restrict__ krow, float (&acc)[CB]) {
+  constexpr int SEGN = (CB + KS - 1 + 3) & ~3;
+  constexpr int NG = (KS + 3) / 4;   // 16-byte groups of the kernel row
   float s[SEGN];
-  float k[KSP];
 #pragma unroll
   for (int i = 0; i < SEGN / 4; ++i) {
     float4 t = reinterpret_cast<const float4*>(seg)[i];
@@ -26,18 +27,20 @@ __device__ __forceinline__ void corr_row(const float* __restrict__ seg,
     s[4 * i + 3] = t.w;
   }
 #pragma unroll
-  for (int i = 0; i < KSP / 4; ++i) {
-    float4 t = reinterpret_cast<const float4*>(krow)[i];
-    k[4 * i] = t.x;
-    k[4 * i + 1] = t.y;
-    k[4 * i + 2] = t.z;
-    k[4 * i + 3] = t.w;
-  }
+  for (int gi = 0; gi < NG; ++gi) {
+    const int g = REV ? NG - 1 - gi : gi;
+    const float4 t = reinterpret_cast<const float4*>(krow)[g];
+    const float kq[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
-  for (int l = 0; l < KS; ++l) {
-    const float kv = REV ? k[KS - 1 - l] : k[l];
+    for (int ei = 0; ei < 4; ++ei) {
+      const int e = REV ? 3 - ei : ei;
+      const int kidx = 4 * g + e;
+      if (kidx < KS) {
+        const int l = REV ? KS - 1 - kidx : kidx;
 #pragma unroll
-    for (int c = 0; c < kColBlock; ++c) acc[c] = fmaf(kv, s[c + l], acc[c]);
+        for (int c = 0; c < CB; ++c) acc[c] = fmaf(kq[e], s[c + l], acc[c]);
+      }
+    }
   }
 }
 

@@ -157,60 +157,102 @@ __device__ __forceinline__ void block_reduce(float (&v)[NV], SmemStatic& s) {
   __syncthreads();
 }
 
-// Conv unit u -> (row i, first column j0).  Eight consecutive units form two
-// rows x four column blocks, which keeps 16-byte shared loads conflict-free
-// when the plane pitch is an odd multiple of four floats.
-__device__ __forceinline__ void unit_coords(const DevImage& I, int u, int& i, int& j0) {
-  int pair = u / (2 * I.ncb);
-  int rem = u - pair * 2 * I.ncb;
-  int cbh = rem >> 3, rsub = (rem >> 2) & 1, cbl = rem & 3;
-  i = 2 * pair + rsub;
-  j0 = kColBlock * (4 * cbh + cbl);
+// Correlation work items (phases 2 and 3).  An item is one warp's work: its
+// four quarter-warps take the four parity planes (ss = 2) of one group of 8
+// units, or four groups of the single plane (ss = 1).  A group is 4 rows x 2
+// column blocks of kFusedCB outputs, so the 16-byte shared loads of a
+// quarter-warp are conflict-free when the plane pitch is an odd multiple of
+// four floats.  Items go to warps round-robin: with 16 warps every SM
+// sub-partition receives the same number of items to within one.
+__device__ __forceinline__ int conv_items(const DevImage& I) {
+  const int groups = ((I.N + 3) >> 2) * (I.ncb >> 1);
+  return I.nplanes == 1 ? (groups + 3) >> 2 : groups;
+}
+
+__device__ __forceinline__ bool conv_unit(const DevImage& I, int item, int lane, int& i, int& j0,
+                                          int& pq) {
+  const int qtr = lane >> 3, l8 = lane & 7;
+  const int pairs = I.ncb >> 1;
+  const int groups = ((I.N + 3) >> 2) * pairs;
+  int g;
+  if (I.nplanes == 1) {
+    g = 4 * item + qtr;
+    pq = 0;
+  } else {
+    g = item;
+    pq = qtr;
+  }
+  const int quad = g / pairs;
+  i = 4 * quad + (l8 >> 1);
+  j0 = kFusedCB * (2 * (g - quad * pairs) + (l8 & 1));
+  return g < groups && i < I.N && j0 < I.N;
 }
 
 // Phase 2: PSF + binning + likelihood.  Returns per-thread partial sums.
+// With four planes the quarter-warps' partial outputs are combined by a
+// reduce-scatter in a fixed order: quarter j ends with outputs 4j..4j+3 of
+// its 16-column block, (a_j + a_{j^2}) + (a_{j^1} + a_{j^3}).
 template <int KS>
 __device__ void phase_conv_forward(const DevImage& I, float* sm, float* img_out, bool want_w,
                                    float& lsum, float& csum) {
-  const int units = I.rows2 * I.ncb;
-  for (int u = threadIdx.x; u < units; u += kThreads) {
-    int i, j0;
-    unit_coords(I, u, i, j0);
-    if (i >= I.N || j0 >= I.N) continue;
-    float acc[kColBlock];
+  const int lane = threadIdx.x & 31, qtr = lane >> 3;
+  const int items = conv_items(I);
+  auto emit = [&](int i, int j, float val) {
+    if (j >= I.N) return;
+    const float im = val * I.cf;
+    if (img_out) img_out[i * I.N + j] = im;
+    if (I.obs) {
+      const float o = __ldg(I.obs + i * I.N + j);
+      const float e2 = I.bg2 + fmaxf(im, 0.f) * I.inv_t;
+      const float err = sqrtf(e2);
+      const float zz = (o - im) / err;
+      lsum += -0.5f * zz * zz - logf(err) - kHalfLog2Pi;
+      csum += zz * zz;
+      if (want_w) {
+        const float inv_e = 1.f / err;
+        float w = zz * inv_e;
+        if (im >= 0.f) w += (zz * zz - 1.f) * 0.5f * inv_e * inv_e * I.inv_t;
+        sm[I.offW + i * I.pitchW + I.padW + j] = w * I.cf;
+      }
+    }
+  };
+  for (int it = threadIdx.x >> 5; it < items; it += kWarps) {
+    int i, j0, pq;
+    const bool valid = conv_unit(I, it, lane, i, j0, pq);
+    float acc[kFusedCB];
 #pragma unroll
-    for (int c = 0; c < kColBlock; ++c) acc[c] = 0.f;
-    for (int pq = 0; pq < I.nplanes; ++pq) {
+    for (int c = 0; c < kFusedCB; ++c) acc[c] = 0.f;
+    if (valid) {
       const int p = pq / I.ss, q = pq - p * I.ss;
       const float* plane = sm + I.offI + pq * I.N * I.pitchI + I.padI[q] - I.d[q] + j0;
       const float* kp = sm + I.offK + pq * KS * I.ksp;
       const int mlo = max(0, I.d[p] - i), mhi = min(KS, I.N + I.d[p] - i);
 #pragma unroll 1
       for (int m = mlo; m < mhi; ++m)
-        corr_row<KS, false>(plane + (i + m - I.d[p]) * I.pitchI, kp + m * I.ksp, acc);
+        corr_row<KS, false, kFusedCB>(plane + (i + m - I.d[p]) * I.pitchI, kp + m * I.ksp, acc);
     }
-    const float* ob = I.obs ? I.obs + i * I.N : nullptr;
+    if (I.nplanes == 4) {
+      float r8[8], r4[4];
+      const bool hi1 = qtr >= 2, hi2 = (qtr & 1) != 0;
 #pragma unroll
-    for (int c = 0; c < kColBlock; ++c) {
-      const int j = j0 + c;
-      if (j < I.N) {
-        const float im = acc[c] * I.cf;
-        if (img_out) img_out[i * I.N + j] = im;
-        if (ob) {
-          const float o = __ldg(ob + j);
-          const float e2 = I.bg2 + fmaxf(im, 0.f) * I.inv_t;
-          const float err = sqrtf(e2);
-          const float zz = (o - im) / err;
-          lsum += -0.5f * zz * zz - logf(err) - kHalfLog2Pi;
-          csum += zz * zz;
-          if (want_w) {
-            const float inv_e = 1.f / err;
-            float w = zz * inv_e;
-            if (im >= 0.f) w += (zz * zz - 1.f) * 0.5f * inv_e * inv_e * I.inv_t;
-            sm[I.offW + i * I.pitchW + I.padW + j] = w * I.cf;
-          }
-        }
+      for (int c = 0; c < 8; ++c) {
+        const float send = hi1 ? acc[c] : acc[c + 8];
+        const float keep = hi1 ? acc[c + 8] : acc[c];
+        r8[c] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
       }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float send = hi2 ? r8[c] : r8[c + 4];
+        const float keep = hi2 ? r8[c + 4] : r8[c];
+        r4[c] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+      }
+      if (valid) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) emit(i, j0 + 4 * qtr + c, r4[c]);
+      }
+    } else if (valid) {
+#pragma unroll
+      for (int c = 0; c < kFusedCB; ++c) emit(i, j0 + c, acc[c]);
     }
   }
 }
@@ -218,27 +260,25 @@ __device__ void phase_conv_forward(const DevImage& I, float* sm, float* img_out,
 // Phase 3: transposed correlation, adjoint image -> supersampled parity planes.
 template <int KS>
 __device__ void phase_conv_adjoint(const DevImage& I, float* sm) {
-  const int units = I.rows2 * I.ncb;
-  const int total = I.nplanes * units;
-  for (int uu = threadIdx.x; uu < total; uu += kThreads) {
-    const int pq = uu / units;
-    int Y, j0;
-    unit_coords(I, uu - pq * units, Y, j0);
-    if (Y >= I.N || j0 >= I.N) continue;
+  const int lane = threadIdx.x & 31;
+  const int items = conv_items(I);
+  for (int it = threadIdx.x >> 5; it < items; it += kWarps) {
+    int Y, j0, pq;
+    if (!conv_unit(I, it, lane, Y, j0, pq)) continue;
     const int p = pq / I.ss, q = pq - p * I.ss;
     const int ep = KS - 1 - I.d[p], eq = KS - 1 - I.d[q];
-    float acc[kColBlock];
+    float acc[kFusedCB];
 #pragma unroll
-    for (int c = 0; c < kColBlock; ++c) acc[c] = 0.f;
+    for (int c = 0; c < kFusedCB; ++c) acc[c] = 0.f;
     const float* wb = sm + I.offW + I.padW - eq + j0;
     const float* kp = sm + I.offK + pq * KS * I.ksp;
     const int mlo = max(0, ep - Y), mhi = min(KS, I.N + ep - Y);
 #pragma unroll 1
     for (int m = mlo; m < mhi; ++m)
-      corr_row<KS, true>(wb + (Y + m - ep) * I.pitchW, kp + (KS - 1 - m) * I.ksp, acc);
+      corr_row<KS, true, kFusedCB>(wb + (Y + m - ep) * I.pitchW, kp + (KS - 1 - m) * I.ksp, acc);
     float* dst = sm + I.offI + pq * I.N * I.pitchI + Y * I.pitchI + I.padI[q] + j0;
 #pragma unroll
-    for (int c = 0; c < kColBlock; ++c)
+    for (int c = 0; c < kFusedCB; ++c)
       if (j0 + c < I.N) dst[c] = acc[c];
   }
 }
@@ -283,40 +323,35 @@ __device__ void phase_pixels_forward(const FusedArgs& a, const DevImage& I, floa
                                      const SmemStatic& st, int K) {
   using T = FamTraits<FAM>;
   const SampleConsts<FAM> c = make_consts<FAM>(a, st.x, K);
-  const int NN = I.N * I.N;
-  const int total = I.nplanes * NN;
-  const float2* grid = reinterpret_cast<const float2*>(I.grid);
+  const int total = I.nplanes * I.N * I.N;
+  const float4* grid = reinterpret_cast<const float4*>(I.grid);
   // light of one pixel from its coordinates and deflection, stored to its plane
-  auto finish = [&](int v, float2 xy, float ax, float ay) {
-    const int pq = v / NN;
-    const int r = v - pq * NN;
-    const int Y = r / I.N, X = r - Y * I.N;
-    const int q = pq - (pq / I.ss) * I.ss;
-    float bx = xy.x - ax, by = xy.y - ay;
+  auto finish = [&](const float4& g, float ax, float ay) {
+    float bx = g.x - ax, by = g.y - ay;
     if (T::kShear) {
-      bx = bx - (c.g1 * xy.x + c.g2 * xy.y);
-      by = by - (c.g2 * xy.x - c.g1 * xy.y);
+      bx = bx - (c.g1 * g.x + c.g2 * g.y);
+      by = by - (c.g2 * g.x - c.g1 * g.y);
     }
     float img = 0.f;
-    if (T::kLensLight) img += sersic_light(c.ll, xy.x, xy.y);
+    if (T::kLensLight) img += sersic_light(c.ll, g.x, g.y);
     img += sersic_light(c.src, bx, by);
     if (isnan(img)) img = 0.f;
-    sm[I.offI + pq * I.N * I.pitchI + Y * I.pitchI + I.padI[q] + X] = img;
+    sm[__float_as_int(g.z)] = img;
   };
   // two pixels per iteration: their series evaluations interleave
   int v = threadIdx.x;
   for (; v + kThreads < total; v += 2 * kThreads) {
-    const float2 xy0 = __ldg(grid + v), xy1 = __ldg(grid + v + kThreads);
+    const float4 g0 = __ldg(grid + v), g1 = __ldg(grid + v + kThreads);
     float ax0, ay0, ax1, ay1;
-    epl_deflect2(c.epl, st.tab, xy0.x, xy0.y, xy1.x, xy1.y, ax0, ay0, ax1, ay1);
-    finish(v, xy0, ax0, ay0);
-    finish(v + kThreads, xy1, ax1, ay1);
+    epl_deflect2(c.epl, st.tab, g0.x, g0.y, g1.x, g1.y, ax0, ay0, ax1, ay1);
+    finish(g0, ax0, ay0);
+    finish(g1, ax1, ay1);
   }
   if (v < total) {
-    const float2 xy = __ldg(grid + v);
+    const float4 g = __ldg(grid + v);
     float ax, ay;
-    epl_deflect(c.epl, st.tab, xy.x, xy.y, ax, ay);
-    finish(v, xy, ax, ay);
+    epl_deflect(c.epl, st.tab, g.x, g.y, ax, ay);
+    finish(g, ax, ay);
   }
 }
 
@@ -341,16 +376,11 @@ __device__ void phase_pixels_reverse(const FusedArgs& a, const DevImage& I, cons
   la.zero();
   sa.zero();
   float g1b = 0.f, g2b = 0.f;
-  const int NN = I.N * I.N;
-  const int total = I.nplanes * NN;
-  const float2* grid = reinterpret_cast<const float2*>(I.grid);
+  const int total = I.nplanes * I.N * I.N;
+  const float4* grid = reinterpret_cast<const float4*>(I.grid);
   for (int v = threadIdx.x; v < total; v += kThreads) {
-    const int pq = v / NN;
-    const int r = v - pq * NN;
-    const int Y = r / I.N, X = r - Y * I.N;
-    const int q = pq - (pq / I.ss) * I.ss;
-    const float gimg = sm[I.offI + pq * I.N * I.pitchI + Y * I.pitchI + I.padI[q] + X];
-    const float2 xy = __ldg(grid + v);
+    const float4 xy = __ldg(grid + v);
+    const float gimg = sm[__float_as_int(xy.z)];
     const EplState es = epl_state(c.epl, st.tab, xy.x, xy.y);
     float bx = xy.x - es.ax, by = xy.y - es.ay;
     if (T::kShear) {

@@ -7,8 +7,10 @@
 
 namespace gl {
 
-constexpr int kThreads = 544;        // 17 warps: 1080 conv units of a 90x90 image in 2 rounds
-constexpr int kColBlock = 8;         // output columns per thread in the PSF correlation
+constexpr int kThreads = 512;        // 16 warps: 4 per SM sub-partition, up to 128 registers
+constexpr int kWarps = kThreads / 32;
+constexpr int kColBlock = 8;         // output columns per thread, least-squares PSF correlation
+constexpr int kFusedCB = 16;         // output columns per thread, fused-kernel PSF correlation
 constexpr int kMaxTerms = 256;       // largest EPL iteration cap the fused kernel accepts
 constexpr int kMaxKS = 25;           // largest parity sub-kernel side
 constexpr int kMaxPlanes = 4;        // supersample <= 2 in the fused kernel
@@ -26,14 +28,15 @@ struct DevImage {
   int padI[kMaxPlanes];   // left zero pad of plane with column parity q
   int pitchW;       // row pitch of the likelihood-adjoint plane
   int padW;         // its left zero pad
-  int ncb;          // column blocks of kColBlock outputs (multiple of 4)
-  int rows2;        // N rounded up to even
+  int ncb;          // column blocks of kFusedCB outputs (even)
+  int units;        // correlation work units of one plane: N rows x ncb blocks
   float x0, y0, t00, t01, t10, t11;   // fine grid: x = t00*col + t01*row + x0
   float cf;         // det(transform_pix2angle), tf/simulator.py:24-26
   float bg2;        // background_rms^2
   float inv_t;      // 1/exp_time
   const float* obs; // device N*N (may be null)
-  const float* grid;// device [nplanes][N][N][2]: (x, y) of each supersampled pixel, plane order
+  const float* grid;// device [nplanes][N][N] float4: (x, y, shared-memory offset of the pixel
+                    // in the fused kernel's parity planes as int bits, 0), plane order
   const float* kern;// device [nplanes][KS][ksp] forward parity sub-kernels
   // shared-memory layout (float offsets)
   int offI, offW, offK, smem_floats;

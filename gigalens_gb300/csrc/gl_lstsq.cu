@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
                                  lpget(st.x, e[3], 0.f), lpget(st.x, e[4], 0.f), lpget(st.x, e[5], 0.f), K);
       const float g1 = a.has_shear ? lpget(st.x, a.shear.col[0], 0.f) : 0.f;
       const float g2 = a.has_shear ? lpget(st.x, a.shear.col[1], 0.f) : 0.f;
-      const float2* grid = reinterpret_cast<const float2*>(I.grid);
+      const float4* grid = reinterpret_cast<const float4*>(I.grid);
       float2* beta = reinterpret_cast<float2*>(sm + I.offB);
       const int per_plane = I.brows * I.N;
       for (int v = tid; v < I.nplanes * per_plane; v += kThreads) {
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
         const int Y = Ylo + yr;
         float2 bt = make_float2(0.f, 0.f);
         if (Y >= 0 && Y < I.N) {
-          const float2 xy = __ldg(grid + ((size_t)pq * I.N + Y) * I.N + X);
+          const float4 xy = __ldg(grid + ((size_t)pq * I.N + Y) * I.N + X);
           float ax, ay;
           epl_deflect(ec, st.tab, xy.x, xy.y, ax, ay);
           bt.x = xy.x - ax;
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
       // evaluate channels c0 .. c0+CPn-1 on the band
       const int per_plane = I.brows * I.N;
       const float2* beta = reinterpret_cast<const float2*>(sm + I.offB);
-      const float2* grid = reinterpret_cast<const float2*>(I.grid);
+      const float4* grid = reinterpret_cast<const float4*>(I.grid);
       for (int v = tid; v < I.CPn * I.nplanes * per_plane; v += kThreads) {
         const int slot = v / (I.nplanes * per_plane);
         const int c = c0 + slot;
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
           px = bt.x;
           py = bt.y;
         } else {
-          const float2 xy = __ldg(grid + ((size_t)pq * I.N + Y) * I.N + X);
+          const float4 xy = __ldg(grid + ((size_t)pq * I.N + Y) * I.N + X);
           px = xy.x;
           py = xy.y;
         }
