@@ -396,7 +396,7 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
   int dev_smem = 0;
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
   plan->smem_bytes = smem_floats * 4;
-  const int static_smem = 8 * 1024;   // SmemStatic upper bound
+  const int static_smem = lsq_model ? 0 : fused_static_smem_bytes();
   if (!lsq_model && plan->smem_bytes + static_smem > dev_smem) {
     set_error("image needs %d bytes of shared memory; the device allows %d per block",
               plan->smem_bytes + static_smem, dev_smem);

@@ -49,7 +49,7 @@ struct SmemStatic {
   float x[GL_MAX_PARAMS];          // physical parameters of the current sample
   float z[GL_MAX_PARAMS];          // unconstrained parameters (z mode)
   float gx[GL_MAX_PARAMS];         // d logL / d x
-  float2 tab[kMaxTerms + 2];       // EPL (p_n, s_n), n = 1..K
+  float4 tab[kMaxTerms + 2];       // EPL series table (A_n, n A_n, s_n A_n, 0), n = 0..K
   float red[kThreads / 32][kRedSlots];
   float out[kRedSlots];
   int K[GL_MAX_IMAGES];
@@ -609,6 +609,22 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
 static int g_sm_count = 0;
 
 static int g_smem_set = -1;   // dynamic smem attribute already set (only ever raised)
+
+// Largest static shared-memory footprint over the fused kernel's families.
+int fused_static_smem_bytes() {
+  int mx = (int)sizeof(SmemStatic);
+  cudaFuncAttributes at;
+  if (cudaFuncGetAttributes(&at, fused_kernel<FAM_EPL_SHEAR_SE_SE>) == cudaSuccess)
+    mx = max(mx, (int)at.sharedSizeBytes);
+  if (cudaFuncGetAttributes(&at, fused_kernel<FAM_EPL_SHEAR_SE>) == cudaSuccess)
+    mx = max(mx, (int)at.sharedSizeBytes);
+  if (cudaFuncGetAttributes(&at, fused_kernel<FAM_EPL_SE_SE>) == cudaSuccess)
+    mx = max(mx, (int)at.sharedSizeBytes);
+  if (cudaFuncGetAttributes(&at, fused_kernel<FAM_EPL_SE>) == cudaSuccess)
+    mx = max(mx, (int)at.sharedSizeBytes);
+  cudaGetLastError();
+  return mx;
+}
 
 int fused_kernel_prepare(int smem_bytes) {
   if (smem_bytes <= g_smem_set) return GL_OK;

@@ -113,6 +113,7 @@ namespace gl {
 // implemented in gl_fused.cu
 int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream);
 int fused_kernel_prepare(int smem_bytes);
+int fused_static_smem_bytes();
 // implemented in gl_profile_eval.cu
 int launch_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,
                         const int* n_terms, float* out0, float* out1, cudaStream_t stream);

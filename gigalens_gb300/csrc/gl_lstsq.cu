@@ -49,7 +49,7 @@ __device__ __forceinline__ float hermite_fn(int n, float u, const float* pref) {
 
 struct LsqShared {
   float x[GL_MAX_PARAMS];
-  float2 tab[kMaxTerms + 2];
+  float4 tab[kMaxTerms + 2];
   float red[kThreads / 32][4];
   int K[GL_MAX_IMAGES];
 };

@@ -9,7 +9,7 @@
 //   Sersic gigalens/tf/profiles/light/sersic.py:25-72
 // The reverse mode is written by hand: it replaces TensorFlow autodiff and
 // differentiates the same expressions.  The EPL series is not stored: its
-// derivatives come from two extra running sums of the recomputed series,
+// derivatives come from two extra sums of the recomputed series,
 //   dF/da = i (2H + F),  H = sum_n n last_n     (last_n = A_n e^{i(2n+1)a})
 //   dF/df = H / f                                (A_n is proportional to f^n)
 //   dF/dt = sum_n s_n last_n, s_n = sum_{m<=n} d ln|p_m| / dt
@@ -113,26 +113,30 @@ __device__ __forceinline__ EplGeom epl_geom(const EplC& c, float x, float y) {
   return g;
 }
 
-// The series as a polynomial: last_n = A_n z^(2n+1) with z = e^{ia},
+// The series as a trigonometric sum: last_n = A_n z^(2n+1) with z = e^{ia},
 // A_n = prod_{m<=n} p_m, so F = sum_{n<=K} last_n = z P(w), P(w) = sum A_n w^n,
-// w = z^2 = e^{2ia}.  tab[n] = (A_n, s_n A_n), n = 0..K (A_0 = 1, s_0 = 0);
-// P is evaluated by Horner's rule (4 FP32 operations per term).
-__device__ __forceinline__ void epl_series_F(const EplGeom& g, const float2* __restrict__ tab, int K,
+// w = z^2 = e^{2ia}.  The coefficients are real and |w| = 1, so
+//   Re P = A_0 + b_1 cos(2a) - b_2,  Im P = b_1 sin(2a),
+//   b_n = A_n + 2 cos(2a) b_{n+1} - b_{n+2}  (n = K..1, b_{K+1} = b_{K+2} = 0),
+// Clenshaw's recurrence: 2 FP32 operations per term and one dependent FMA.
+// tab[n] = (A_n, n A_n, s_n A_n, 0), n = 0..K (A_0 = 1, s_0 = 0).
+__device__ __forceinline__ void epl_series_F(const EplGeom& g, const float4* __restrict__ tab, int K,
                                              float& Fx, float& Fy) {
-  float Px = tab[K].x, Py = 0.f;
+  const float c2 = 2.f * g.Cs2;
+  float b1 = 0.f, b2 = 0.f;
 #pragma unroll 4
-  for (int n = K - 1; n >= 0; --n) {
-    const float a = tab[n].x;
-    const float nx = fmaf(Px, g.Cs2, fmaf(-Py, g.Ss2, a));
-    Py = fmaf(Px, g.Ss2, Py * g.Cs2);
-    Px = nx;
+  for (int n = K; n >= 1; --n) {
+    const float b0 = fmaf(c2, b1, tab[n].x - b2);
+    b2 = b1;
+    b1 = b0;
   }
+  const float Px = fmaf(b1, g.Cs2, 1.f - b2), Py = b1 * g.Ss2;
   Fx = g.Cs * Px - g.Ss * Py;
   Fy = g.Cs * Py + g.Ss * Px;
 }
 
 // Forward deflection.
-__device__ __forceinline__ void epl_deflect(const EplC& c, const float2* __restrict__ tab, float x,
+__device__ __forceinline__ void epl_deflect(const EplC& c, const float4* __restrict__ tab, float x,
                                             float y, float& ax, float& ay) {
   EplGeom g = epl_geom(c, x, y);
   float Fx, Fy;
@@ -143,31 +147,34 @@ __device__ __forceinline__ void epl_deflect(const EplC& c, const float2* __restr
   ay = arx * c.sph + ary * c.cph;
 }
 
-// Two pixels at once (independent Horner chains interleave for ILP).
-__device__ __forceinline__ void epl_deflect2(const EplC& c, const float2* __restrict__ tab, float x0,
+// Two pixels at once (their recurrences interleave for ILP).
+__device__ __forceinline__ void epl_deflect2(const EplC& c, const float4* __restrict__ tab, float x0,
                                              float y0, float x1, float y1, float& ax0, float& ay0,
                                              float& ax1, float& ay1) {
   const EplGeom g0 = epl_geom(c, x0, y0), g1 = epl_geom(c, x1, y1);
-  float P0x = tab[c.K].x, P0y = 0.f, P1x = P0x, P1y = 0.f;
+  const float c20 = 2.f * g0.Cs2, c21 = 2.f * g1.Cs2;
+  float b10 = 0.f, b20 = 0.f, b11 = 0.f, b21 = 0.f;
 #pragma unroll 4
-  for (int n = c.K - 1; n >= 0; --n) {
+  for (int n = c.K; n >= 1; --n) {
     const float a = tab[n].x;
-    const float n0 = fmaf(P0x, g0.Cs2, fmaf(-P0y, g0.Ss2, a));
-    const float n1 = fmaf(P1x, g1.Cs2, fmaf(-P1y, g1.Ss2, a));
-    P0y = fmaf(P0x, g0.Ss2, P0y * g0.Cs2);
-    P1y = fmaf(P1x, g1.Ss2, P1y * g1.Cs2);
-    P0x = n0;
-    P1x = n1;
+    const float n0 = fmaf(c20, b10, a - b20);
+    const float n1 = fmaf(c21, b11, a - b21);
+    b20 = b10;
+    b10 = n0;
+    b21 = b11;
+    b11 = n1;
   }
   {
-    const float Fx = g0.Cs * P0x - g0.Ss * P0y, Fy = g0.Cs * P0y + g0.Ss * P0x;
+    const float Px = fmaf(b10, g0.Cs2, 1.f - b20), Py = b10 * g0.Ss2;
+    const float Fx = g0.Cs * Px - g0.Ss * Py, Fy = g0.Cs * Py + g0.Ss * Px;
     const float P = c.A * exp2f(c.tm1 * (c.log2b - g0.l2Rc));
     const float arx = Fx * P, ary = Fy * P;
     ax0 = arx * c.cph - ary * c.sph;
     ay0 = arx * c.sph + ary * c.cph;
   }
   {
-    const float Fx = g1.Cs * P1x - g1.Ss * P1y, Fy = g1.Cs * P1y + g1.Ss * P1x;
+    const float Px = fmaf(b11, g1.Cs2, 1.f - b21), Py = b11 * g1.Ss2;
+    const float Fx = g1.Cs * Px - g1.Ss * Py, Fy = g1.Cs * Py + g1.Ss * Px;
     const float P = c.A * exp2f(c.tm1 * (c.log2b - g1.l2Rc));
     const float arx = Fx * P, ary = Fy * P;
     ax1 = arx * c.cph - ary * c.sph;
@@ -180,42 +187,43 @@ struct EplAcc {
   __device__ __forceinline__ void zero() { phi = SP = SPlnR = FH = FT = q = cx = cy = 0.f; }
 };
 
-// Series state of one pixel: the deflection plus the running sums that the
-// reverse mode needs (H = sum n last_n, T = sum s_n last_n).
+// Series state of one pixel: the deflection plus the sums that the reverse
+// mode needs (H = sum n last_n, T = sum s_n last_n).
 struct EplState {
   EplGeom g;
   float Fx, Fy, Hx, Hy, Tx, Ty, P, ax, ay;
 };
 
-// F = z P(w), H = sum n last_n = z w P'(w), T = sum s_n last_n = z Q(w) with
-// Q(w) = sum s_n A_n w^n: Horner with derivative, three chains per term.
-__device__ __forceinline__ EplState epl_state(const EplC& c, const float2* __restrict__ tab, float x,
+// F = z P(w), H = z sum n A_n w^n, T = z sum s_n A_n w^n: three Clenshaw
+// recurrences over the columns of the table.
+__device__ __forceinline__ EplState epl_state(const EplC& c, const float4* __restrict__ tab, float x,
                                               float y) {
   EplState s;
   s.g = epl_geom(c, x, y);
-  const float wx = s.g.Cs2, wy = s.g.Ss2;
-  const float2 top = tab[c.K];
-  float Px = top.x, Py = 0.f, Dx = 0.f, Dy = 0.f, Qx = top.y, Qy = 0.f;
+  const float wx = s.g.Cs2, wy = s.g.Ss2, c2 = 2.f * wx;
+  float a1 = 0.f, a2 = 0.f, m1 = 0.f, m2 = 0.f, r1 = 0.f, r2 = 0.f;
 #pragma unroll 2
-  for (int n = c.K - 1; n >= 0; --n) {
-    const float2 ab = tab[n];
-    // D <- D w + P (derivative), then P <- P w + A_n, Q <- Q w + B_n
-    const float dx = fmaf(Dx, wx, fmaf(-Dy, wy, Px));
-    Dy = fmaf(Dx, wy, fmaf(Dy, wx, Py));
-    Dx = dx;
-    const float px = fmaf(Px, wx, fmaf(-Py, wy, ab.x));
-    Py = fmaf(Px, wy, Py * wx);
-    Px = px;
-    const float qx = fmaf(Qx, wx, fmaf(-Qy, wy, ab.y));
-    Qy = fmaf(Qx, wy, Qy * wx);
-    Qx = qx;
+  for (int n = c.K; n >= 1; --n) {
+    const float4 t = tab[n];
+    const float a0 = fmaf(c2, a1, t.x - a2);
+    const float m0 = fmaf(c2, m1, t.y - m2);
+    const float r0 = fmaf(c2, r1, t.z - r2);
+    a2 = a1;
+    a1 = a0;
+    m2 = m1;
+    m1 = m0;
+    r2 = r1;
+    r1 = r0;
   }
+  // n = 0 coefficients: A_0 = 1, 0 * A_0 = 0, s_0 A_0 = 0
+  const float Px = fmaf(a1, wx, 1.f - a2), Py = a1 * wy;
+  const float Nx = fmaf(m1, wx, -m2), Ny = m1 * wy;
+  const float Qx = fmaf(r1, wx, -r2), Qy = r1 * wy;
   const float zx = s.g.Cs, zy = s.g.Ss;
   s.Fx = zx * Px - zy * Py;
   s.Fy = zx * Py + zy * Px;
-  const float zwx = zx * wx - zy * wy, zwy = zx * wy + zy * wx;   // z w = z^3
-  s.Hx = zwx * Dx - zwy * Dy;
-  s.Hy = zwx * Dy + zwy * Dx;
+  s.Hx = zx * Nx - zy * Ny;
+  s.Hy = zx * Ny + zy * Nx;
   s.Tx = zx * Qx - zy * Qy;
   s.Ty = zx * Qy + zy * Qx;
   s.P = c.A * exp2f(c.tm1 * (c.log2b - s.g.l2Rc));
@@ -225,10 +233,10 @@ __device__ __forceinline__ EplState epl_state(const EplC& c, const float2* __res
   return s;
 }
 
-// Per-chain series table, built by one warp: tab[n] = (A_n, s_n A_n), n = 0..K,
-// with A_n = prod_{m<=n} p_m (p_m with the reference's op order) and
+// Per-chain series table, built by one warp: tab[n] = (A_n, n A_n, s_n A_n, 0),
+// n = 0..K, with A_n = prod_{m<=n} p_m (p_m with the reference's op order) and
 // s_n = sum_{m<=n} d ln|p_m| / dt, both as warp scans.
-__device__ __forceinline__ void epl_build_table(float2* tab, float f, float t, int K, int lane) {
+__device__ __forceinline__ void epl_build_table(float4* tab, float f, float t, int K, int lane) {
   float carry_p = 1.f, carry_s = 0.f;
   for (int base = 0; base <= K; base += 32) {
     const int n = base + lane;
@@ -245,7 +253,7 @@ __device__ __forceinline__ void epl_build_table(float2* tab, float f, float t, i
       }
     }
     const float A = carry_p * p, S = carry_s + dl;
-    if (n <= K) tab[n] = make_float2(A, S * A);
+    if (n <= K) tab[n] = make_float4(A, (float)n * A, S * A, 0.f);
     carry_p *= __shfl_sync(0xffffffffu, p, 31);
     carry_s += __shfl_sync(0xffffffffu, dl, 31);
   }

@@ -171,8 +171,9 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
         gen.manual_seed(seed)
         lens_sim = LensSimulator(self.phys_model, self.sim_config, bs=n_hmc)
         plan = lens_sim.prob_plan(self.prob_model)
-        cov = q_z.covariance().to(dev, torch.float32)
-        Lq = torch.linalg.cholesky(cov.double()).float()
+        # the guide's Cholesky factor: Sigma = Lq Lq^T without re-factoring Sigma
+        Lq = q_z.scale_tril.to(dev, torch.float32).contiguous()
+        cov = Lq @ Lq.T
         d = cov.shape[0]
         z = q_z.sample(n_hmc, generator=gen).to(dev).contiguous()
         torch.cuda.manual_seed(seed)   # leapfrog draws use the default generator (graph-capturable)
