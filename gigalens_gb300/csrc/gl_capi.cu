@@ -201,7 +201,9 @@ static int build_image(const gl_image_desc& g, DevImage& I, HostImage& hi) {
   I.pitchW = pitch;
   I.offI = 0;
   I.offW = I.nplanes * N * I.pitchI;
-  I.offK = I.offW + N * I.pitchW;
+  // one spare row after the likelihood-adjoint plane: the row prefetch of the
+  // transposed correlation reads one row past the plane's last
+  I.offK = I.offW + (N + 1) * I.pitchW;
   I.smem_floats = I.offK + I.nplanes * KS * I.ksp;
   // coordinate grid, gigalens/simulator.py:91-125 (float64 then float32)
   const int S = ss * N;

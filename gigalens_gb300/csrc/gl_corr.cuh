@@ -44,6 +44,56 @@ __device__ __forceinline__ void corr_row(const float* __restrict__ seg,
   }
 }
 
+// n consecutive rows: acc[c] += sum_r sum_l k_r[l] * seg_r[c + l], with
+// seg_r = seg + r * seg_pitch and k_r = krow + r * k_step (REV: taps reversed).
+// The next row's segment is loaded while the current one is consumed.  The
+// prefetch of row n (one past the last) must stay inside shared memory; its
+// values are not used.
+template <int KS, bool REV, int CB>
+__device__ __forceinline__ void corr_rows(const float* __restrict__ seg, int seg_pitch,
+                                          const float* __restrict__ krow, int k_step, int n,
+                                          float (&acc)[CB]) {
+  constexpr int SEGN = (CB + KS - 1 + 3) & ~3;
+  constexpr int NG = (KS + 3) / 4;
+  float4 cur[SEGN / 4];
+#pragma unroll
+  for (int i = 0; i < SEGN / 4; ++i) cur[i] = reinterpret_cast<const float4*>(seg)[i];
+#pragma unroll 2
+  for (int r = 0; r < n; ++r) {
+    float4 nxt[SEGN / 4];
+    const float4* sn = reinterpret_cast<const float4*>(seg + (r + 1) * seg_pitch);
+#pragma unroll
+    for (int i = 0; i < SEGN / 4; ++i) nxt[i] = sn[i];
+    float s[SEGN];
+#pragma unroll
+    for (int i = 0; i < SEGN / 4; ++i) {
+      s[4 * i] = cur[i].x;
+      s[4 * i + 1] = cur[i].y;
+      s[4 * i + 2] = cur[i].z;
+      s[4 * i + 3] = cur[i].w;
+    }
+    const float* kr = krow + r * k_step;
+#pragma unroll
+    for (int gi = 0; gi < NG; ++gi) {
+      const int g = REV ? NG - 1 - gi : gi;
+      const float4 t = reinterpret_cast<const float4*>(kr)[g];
+      const float kq[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+      for (int ei = 0; ei < 4; ++ei) {
+        const int e = REV ? 3 - ei : ei;
+        const int kidx = 4 * g + e;
+        if (kidx < KS) {
+          const int l = REV ? KS - 1 - kidx : kidx;
+#pragma unroll
+          for (int c = 0; c < CB; ++c) acc[c] = fmaf(kq[e], s[c + l], acc[c]);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < SEGN / 4; ++i) cur[i] = nxt[i];
+  }
+}
+
 #define GL_KS_DISPATCH(KSVAL, CALL) \
   switch (KSVAL) {                  \
     case 1: CALL(1); break;         \

@@ -45,6 +45,10 @@ struct FamTraits<FAM_EPL_SE> {
   static constexpr bool kShear = false, kLensLight = false;
 };
 
+// Pixels per thread whose series recurrences interleave (phase 1, phase 4).
+constexpr int kPixF = 4;
+constexpr int kPixR = 2;
+
 struct SmemStatic {
   float x[GL_MAX_PARAMS];          // physical parameters of the current sample
   float z[GL_MAX_PARAMS];          // unconstrained parameters (z mode)
@@ -227,9 +231,10 @@ __device__ void phase_conv_forward(const DevImage& I, float* sm, float* img_out,
       const float* plane = sm + I.offI + pq * I.N * I.pitchI + I.padI[q] - I.d[q] + j0;
       const float* kp = sm + I.offK + pq * KS * I.ksp;
       const int mlo = max(0, I.d[p] - i), mhi = min(KS, I.N + I.d[p] - i);
-#pragma unroll 1
-      for (int m = mlo; m < mhi; ++m)
-        corr_row<KS, false, kFusedCB>(plane + (i + m - I.d[p]) * I.pitchI, kp + m * I.ksp, acc);
+      // the prefetch one row past mhi reads the next plane, the likelihood
+      // plane or the sub-kernels: all inside shared memory
+      corr_rows<KS, false, kFusedCB>(plane + (i + mlo - I.d[p]) * I.pitchI, I.pitchI, kp + mlo * I.ksp,
+                                     I.ksp, mhi - mlo, acc);
     }
     if (I.nplanes == 4) {
       float r8[8], r4[4];
@@ -273,9 +278,9 @@ __device__ void phase_conv_adjoint(const DevImage& I, float* sm) {
     const float* wb = sm + I.offW + I.padW - eq + j0;
     const float* kp = sm + I.offK + pq * KS * I.ksp;
     const int mlo = max(0, ep - Y), mhi = min(KS, I.N + ep - Y);
-#pragma unroll 1
-    for (int m = mlo; m < mhi; ++m)
-      corr_row<KS, true, kFusedCB>(wb + (Y + m - ep) * I.pitchW, kp + (KS - 1 - m) * I.ksp, acc);
+    // the prefetch one row past mhi reads the spare row after the plane
+    corr_rows<KS, true, kFusedCB>(wb + (Y + mlo - ep) * I.pitchW, I.pitchW, kp + (KS - 1 - mlo) * I.ksp,
+                                  -I.ksp, mhi - mlo, acc);
     float* dst = sm + I.offI + pq * I.N * I.pitchI + Y * I.pitchI + I.padI[q] + j0;
 #pragma unroll
     for (int c = 0; c < kFusedCB; ++c)
@@ -338,20 +343,26 @@ __device__ void phase_pixels_forward(const FusedArgs& a, const DevImage& I, floa
     if (isnan(img)) img = 0.f;
     sm[__float_as_int(g.z)] = img;
   };
-  // two pixels per iteration: their series evaluations interleave
+  // kPixF pixels per iteration: their series evaluations interleave
   int v = threadIdx.x;
-  for (; v + kThreads < total; v += 2 * kThreads) {
-    const float4 g0 = __ldg(grid + v), g1 = __ldg(grid + v + kThreads);
-    float ax0, ay0, ax1, ay1;
-    epl_deflect2(c.epl, st.tab, g0.x, g0.y, g1.x, g1.y, ax0, ay0, ax1, ay1);
-    finish(g0, ax0, ay0);
-    finish(g1, ax1, ay1);
+  for (; v + (kPixF - 1) * kThreads < total; v += kPixF * kThreads) {
+    float4 g[kPixF];
+    float x[kPixF], y[kPixF], ax[kPixF], ay[kPixF];
+#pragma unroll
+    for (int k = 0; k < kPixF; ++k) {
+      g[k] = __ldg(grid + v + k * kThreads);
+      x[k] = g[k].x;
+      y[k] = g[k].y;
+    }
+    epl_deflect_n<kPixF>(c.epl, st.tab, x, y, ax, ay);
+#pragma unroll
+    for (int k = 0; k < kPixF; ++k) finish(g[k], ax[k], ay[k]);
   }
-  if (v < total) {
+  for (; v < total; v += kThreads) {
     const float4 g = __ldg(grid + v);
-    float ax, ay;
-    epl_deflect(c.epl, st.tab, g.x, g.y, ax, ay);
-    finish(g, ax, ay);
+    float x[1] = {g.x}, y[1] = {g.y}, ax[1], ay[1];
+    epl_deflect_n<1>(c.epl, st.tab, x, y, ax, ay);
+    finish(g, ax[0], ay[0]);
   }
 }
 
@@ -378,10 +389,8 @@ __device__ void phase_pixels_reverse(const FusedArgs& a, const DevImage& I, cons
   float g1b = 0.f, g2b = 0.f;
   const int total = I.nplanes * I.N * I.N;
   const float4* grid = reinterpret_cast<const float4*>(I.grid);
-  for (int v = threadIdx.x; v < total; v += kThreads) {
-    const float4 xy = __ldg(grid + v);
-    const float gimg = sm[__float_as_int(xy.z)];
-    const EplState es = epl_state(c.epl, st.tab, xy.x, xy.y);
+  // light reverse and parameter accumulation of one pixel
+  auto pixel = [&](const float4& xy, float gimg, const EplState& es) {
     float bx = xy.x - es.ax, by = xy.y - es.ay;
     if (T::kShear) {
       bx = bx - (c.g1 * xy.x + c.g2 * xy.y);
@@ -395,7 +404,7 @@ __device__ void phase_pixels_reverse(const FusedArgs& a, const DevImage& I, cons
     }
     const SerFwd sf = sersic_fwd(c.src, bx, by);
     img += sf.I;
-    if (isnan(img)) continue;   // the reference zeroes NaN pixels: no gradient flows
+    if (isnan(img)) return;   // the reference zeroes NaN pixels: no gradient flows
     float dummyx, dummyy, bxb, byb;
     if (T::kLensLight) sersic_reverse(c.ll, lf, gimg, la, dummyx, dummyy);
     sersic_reverse(c.src, sf, gimg, sa, bxb, byb);
@@ -405,6 +414,27 @@ __device__ void phase_pixels_reverse(const FusedArgs& a, const DevImage& I, cons
       g2b += abx * xy.y + aby * xy.x;
     }
     epl_backprop(c.epl, es, abx, aby, ea);
+  };
+  // kPixR pixels per iteration: their series recurrences interleave
+  int px = threadIdx.x;
+  for (; px + (kPixR - 1) * kThreads < total; px += kPixR * kThreads) {
+    float4 g[kPixR];
+    float x[kPixR], y[kPixR], gi[kPixR];
+#pragma unroll
+    for (int k = 0; k < kPixR; ++k) {
+      g[k] = __ldg(grid + px + k * kThreads);
+      x[k] = g[k].x;
+      y[k] = g[k].y;
+      gi[k] = sm[__float_as_int(g[k].z)];
+    }
+    EplState es[kPixR];
+    epl_state_n<kPixR>(c.epl, st.tab, x, y, es);
+#pragma unroll
+    for (int k = 0; k < kPixR; ++k) pixel(g[k], gi[k], es[k]);
+  }
+  for (; px < total; px += kThreads) {
+    const float4 g = __ldg(grid + px);
+    pixel(g, sm[__float_as_int(g.z)], epl_state(c.epl, st.tab, g.x, g.y));
   }
   float v[R_NACC] = {ea.phi, ea.SP, ea.SPlnR, ea.FH, ea.FT, ea.q, ea.cx, ea.cy,
                      g1b, g2b,

@@ -147,38 +147,38 @@ __device__ __forceinline__ void epl_deflect(const EplC& c, const float4* __restr
   ay = arx * c.sph + ary * c.cph;
 }
 
-// Two pixels at once (their recurrences interleave for ILP).
-__device__ __forceinline__ void epl_deflect2(const EplC& c, const float4* __restrict__ tab, float x0,
-                                             float y0, float x1, float y1, float& ax0, float& ay0,
-                                             float& ax1, float& ay1) {
-  const EplGeom g0 = epl_geom(c, x0, y0), g1 = epl_geom(c, x1, y1);
-  const float c20 = 2.f * g0.Cs2, c21 = 2.f * g1.Cs2;
-  float b10 = 0.f, b20 = 0.f, b11 = 0.f, b21 = 0.f;
-#pragma unroll 4
+// NP pixels at once: their recurrences interleave for ILP.
+template <int NP>
+__device__ __forceinline__ void epl_deflect_n(const EplC& c, const float4* __restrict__ tab,
+                                              const float (&x)[NP], const float (&y)[NP],
+                                              float (&ax)[NP], float (&ay)[NP]) {
+  EplGeom g[NP];
+  float c2[NP], b1[NP], b2[NP];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    g[k] = epl_geom(c, x[k], y[k]);
+    c2[k] = 2.f * g[k].Cs2;
+    b1[k] = 0.f;
+    b2[k] = 0.f;
+  }
+#pragma unroll 2
   for (int n = c.K; n >= 1; --n) {
     const float a = tab[n].x;
-    const float n0 = fmaf(c20, b10, a - b20);
-    const float n1 = fmaf(c21, b11, a - b21);
-    b20 = b10;
-    b10 = n0;
-    b21 = b11;
-    b11 = n1;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      const float b0 = fmaf(c2[k], b1[k], a - b2[k]);
+      b2[k] = b1[k];
+      b1[k] = b0;
+    }
   }
-  {
-    const float Px = fmaf(b10, g0.Cs2, 1.f - b20), Py = b10 * g0.Ss2;
-    const float Fx = g0.Cs * Px - g0.Ss * Py, Fy = g0.Cs * Py + g0.Ss * Px;
-    const float P = c.A * exp2f(c.tm1 * (c.log2b - g0.l2Rc));
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    const float Px = fmaf(b1[k], g[k].Cs2, 1.f - b2[k]), Py = b1[k] * g[k].Ss2;
+    const float Fx = g[k].Cs * Px - g[k].Ss * Py, Fy = g[k].Cs * Py + g[k].Ss * Px;
+    const float P = c.A * exp2f(c.tm1 * (c.log2b - g[k].l2Rc));
     const float arx = Fx * P, ary = Fy * P;
-    ax0 = arx * c.cph - ary * c.sph;
-    ay0 = arx * c.sph + ary * c.cph;
-  }
-  {
-    const float Px = fmaf(b11, g1.Cs2, 1.f - b21), Py = b11 * g1.Ss2;
-    const float Fx = g1.Cs * Px - g1.Ss * Py, Fy = g1.Cs * Py + g1.Ss * Px;
-    const float P = c.A * exp2f(c.tm1 * (c.log2b - g1.l2Rc));
-    const float arx = Fx * P, ary = Fy * P;
-    ax1 = arx * c.cph - ary * c.sph;
-    ay1 = arx * c.sph + ary * c.cph;
+    ax[k] = arx * c.cph - ary * c.sph;
+    ay[k] = arx * c.sph + ary * c.cph;
   }
 }
 
@@ -195,42 +195,61 @@ struct EplState {
 };
 
 // F = z P(w), H = z sum n A_n w^n, T = z sum s_n A_n w^n: three Clenshaw
-// recurrences over the columns of the table.
-__device__ __forceinline__ EplState epl_state(const EplC& c, const float4* __restrict__ tab, float x,
-                                              float y) {
-  EplState s;
-  s.g = epl_geom(c, x, y);
-  const float wx = s.g.Cs2, wy = s.g.Ss2, c2 = 2.f * wx;
-  float a1 = 0.f, a2 = 0.f, m1 = 0.f, m2 = 0.f, r1 = 0.f, r2 = 0.f;
+// recurrences over the columns of the table, for NP pixels at once.
+template <int NP>
+__device__ __forceinline__ void epl_state_n(const EplC& c, const float4* __restrict__ tab,
+                                            const float (&x)[NP], const float (&y)[NP],
+                                            EplState (&s)[NP]) {
+  float c2[NP], a1[NP], a2[NP], m1[NP], m2[NP], r1[NP], r2[NP];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    s[k].g = epl_geom(c, x[k], y[k]);
+    c2[k] = 2.f * s[k].g.Cs2;
+    a1[k] = a2[k] = m1[k] = m2[k] = r1[k] = r2[k] = 0.f;
+  }
 #pragma unroll 2
   for (int n = c.K; n >= 1; --n) {
     const float4 t = tab[n];
-    const float a0 = fmaf(c2, a1, t.x - a2);
-    const float m0 = fmaf(c2, m1, t.y - m2);
-    const float r0 = fmaf(c2, r1, t.z - r2);
-    a2 = a1;
-    a1 = a0;
-    m2 = m1;
-    m1 = m0;
-    r2 = r1;
-    r1 = r0;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      const float a0 = fmaf(c2[k], a1[k], t.x - a2[k]);
+      const float m0 = fmaf(c2[k], m1[k], t.y - m2[k]);
+      const float r0 = fmaf(c2[k], r1[k], t.z - r2[k]);
+      a2[k] = a1[k];
+      a1[k] = a0;
+      m2[k] = m1[k];
+      m1[k] = m0;
+      r2[k] = r1[k];
+      r1[k] = r0;
+    }
   }
-  // n = 0 coefficients: A_0 = 1, 0 * A_0 = 0, s_0 A_0 = 0
-  const float Px = fmaf(a1, wx, 1.f - a2), Py = a1 * wy;
-  const float Nx = fmaf(m1, wx, -m2), Ny = m1 * wy;
-  const float Qx = fmaf(r1, wx, -r2), Qy = r1 * wy;
-  const float zx = s.g.Cs, zy = s.g.Ss;
-  s.Fx = zx * Px - zy * Py;
-  s.Fy = zx * Py + zy * Px;
-  s.Hx = zx * Nx - zy * Ny;
-  s.Hy = zx * Ny + zy * Nx;
-  s.Tx = zx * Qx - zy * Qy;
-  s.Ty = zx * Qy + zy * Qx;
-  s.P = c.A * exp2f(c.tm1 * (c.log2b - s.g.l2Rc));
-  float arx = s.Fx * s.P, ary = s.Fy * s.P;
-  s.ax = arx * c.cph - ary * c.sph;
-  s.ay = arx * c.sph + ary * c.cph;
-  return s;
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    const float wx = s[k].g.Cs2, wy = s[k].g.Ss2;
+    // n = 0 coefficients: A_0 = 1, 0 * A_0 = 0, s_0 A_0 = 0
+    const float Px = fmaf(a1[k], wx, 1.f - a2[k]), Py = a1[k] * wy;
+    const float Nx = fmaf(m1[k], wx, -m2[k]), Ny = m1[k] * wy;
+    const float Qx = fmaf(r1[k], wx, -r2[k]), Qy = r1[k] * wy;
+    const float zx = s[k].g.Cs, zy = s[k].g.Ss;
+    s[k].Fx = zx * Px - zy * Py;
+    s[k].Fy = zx * Py + zy * Px;
+    s[k].Hx = zx * Nx - zy * Ny;
+    s[k].Hy = zx * Ny + zy * Nx;
+    s[k].Tx = zx * Qx - zy * Qy;
+    s[k].Ty = zx * Qy + zy * Qx;
+    s[k].P = c.A * exp2f(c.tm1 * (c.log2b - s[k].g.l2Rc));
+    const float arx = s[k].Fx * s[k].P, ary = s[k].Fy * s[k].P;
+    s[k].ax = arx * c.cph - ary * c.sph;
+    s[k].ay = arx * c.sph + ary * c.cph;
+  }
+}
+
+__device__ __forceinline__ EplState epl_state(const EplC& c, const float4* __restrict__ tab, float x,
+                                              float y) {
+  const float xs[1] = {x}, ys[1] = {y};
+  EplState s[1];
+  epl_state_n<1>(c, tab, xs, ys, s);
+  return s[0];
 }
 
 // Per-chain series table, built by one warp: tab[n] = (A_n, n A_n, s_n A_n, 0),
