@@ -64,7 +64,7 @@ def build(force=False, verbose=False, ptxas_info=False):
             sys.stderr.write(r.stdout + r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
+    with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         objs = list(ex.map(compile_one, sources()))
     tmp = LIB + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]

@@ -10,6 +10,8 @@ import threading
 
 from . import _build
 
+GL_ABI_VERSION = 2   # include/gigalens_cuda.h
+
 GL_OK = 0
 GL_ERR_INVALID = -1
 GL_ERR_UNSUPPORTED = -2
@@ -21,16 +23,18 @@ GL_PROF_EPL = 1
 GL_PROF_SHEAR = 2
 GL_PROF_SIS = 3
 GL_PROF_SIE = 4
+GL_PROF_TNFW = 5
 GL_PROF_SERSIC = 10
 GL_PROF_SERSIC_ELLIPSE = 11
 GL_PROF_SHAPELETS = 12
+GL_PROF_CORE_SERSIC = 13
 
 GL_GROUP_LENS = 0
 GL_GROUP_LENS_LIGHT = 1
 GL_GROUP_SOURCE = 2
 
 GL_MAX_PROFILES = 8
-GL_MAX_PROFILE_PARAMS = 8
+GL_MAX_PROFILE_PARAMS = 12
 GL_MAX_IMAGES = 8
 GL_MAX_PARAMS = 64
 
@@ -44,9 +48,11 @@ PROFILE_TYPES = {
     "SHEAR": GL_PROF_SHEAR,
     "SIS": GL_PROF_SIS,
     "SIE": GL_PROF_SIE,
+    "TNFW": GL_PROF_TNFW,
     "SERSIC": GL_PROF_SERSIC,
     "SERSIC_ELLIPSE": GL_PROF_SERSIC_ELLIPSE,
     "SHAPELETS": GL_PROF_SHAPELETS,
+    "CORE_SERSIC": GL_PROF_CORE_SERSIC,
 }
 
 # canonical parameter order of each type (the header's table)
@@ -56,8 +62,10 @@ CANONICAL_PARAMS = {
     "SIS": ["theta_E", "center_x", "center_y"],
     "SIE": ["theta_E", "e1", "e2", "center_x", "center_y"],
     "SERSIC": ["R_sersic", "n_sersic", "center_x", "center_y", "Ie"],
+    "TNFW": ["Rs", "alpha_Rs", "r_trunc", "center_x", "center_y"],
     "SERSIC_ELLIPSE": ["R_sersic", "n_sersic", "e1", "e2", "center_x", "center_y", "Ie"],
-    "SHAPELETS": ["beta", "center_x", "center_y"],
+    "CORE_SERSIC": ["R_sersic", "n_sersic", "Rb", "alpha", "gamma", "e1", "e2", "center_x", "center_y", "Ie"],
+    "SHAPELETS": ["beta", "center_x", "center_y"],   # + amp0: first amplitude column (see _plan)
 }
 
 
@@ -147,6 +155,7 @@ SIGNATURES = [
     ("gl_lstsq_workspace", _i, [_vp, _i, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_i)]),
     ("gl_lstsq", _i, [_vp, _vp, _vp, _i, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp]),
     ("gl_lstsq_noalloc", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    ("gl_lstsq_grad", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
     ("gl_nn_gemm", _i, [_i, _i, _i, _i, _i, _i, ctypes.c_float, _vp, _i, ctypes.c_longlong, _vp, _i,
                         ctypes.c_longlong, ctypes.c_float, _vp, _i, ctypes.c_longlong, _i, _i, _vp]),
     ("gl_nn_im2col3x3", _i, [_vp, _i, _i, _i, _i, _i, _vp, _vp]),
@@ -189,6 +198,9 @@ def lib():
                 fn = getattr(handle, name)
                 fn.restype = res
                 fn.argtypes = args
+            if handle.gl_abi_version() != GL_ABI_VERSION:
+                raise RuntimeError("%s has ABI version %d, this binding expects %d: rebuild it"
+                                   % (_build.LIB, handle.gl_abi_version(), GL_ABI_VERSION))
             _lib = handle
     return _lib
 

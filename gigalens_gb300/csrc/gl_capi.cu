@@ -36,18 +36,21 @@ static int param_count(int type) {
     case GL_PROF_SHEAR: return 2;
     case GL_PROF_SIS: return 3;
     case GL_PROF_SIE: return 5;
+    case GL_PROF_TNFW: return 5;
     case GL_PROF_SERSIC: return 5;
     case GL_PROF_SERSIC_ELLIPSE: return 7;
-    case GL_PROF_SHAPELETS: return 3;
+    case GL_PROF_CORE_SERSIC: return 10;
+    case GL_PROF_SHAPELETS: return 4;
     default: return -1;
   }
 }
 
-// Map the model descriptor to a compiled family of the fused kernel and
-// resolve every slot to flat-vector columns.  SERSIC (spherical) runs as
-// SERSIC_ELLIPSE with e1 = e2 = 0.
-static int resolve_family(const gl_model_desc* m, int* family, DevProfile* epl, DevProfile* shear,
-                          DevProfile* llight, DevProfile* source) {
+// Map the model descriptor to a compiled fast-path family of the fused kernel
+// and resolve every slot to flat-vector columns.  SERSIC (spherical) runs as
+// SERSIC_ELLIPSE with e1 = e2 = 0.  Returns false (no error) when the model
+// is not one of the fast-path families.
+static bool resolve_family(const gl_model_desc* m, int* family, DevProfile* epl, DevProfile* shear,
+                           DevProfile* llight, DevProfile* source) {
   int n_epl = 0, n_shear = 0, n_ll = 0, n_src = 0;
   for (auto* p : {epl, shear, llight, source}) {
     p->type = GL_PROF_NONE;
@@ -67,14 +70,14 @@ static int resolve_family(const gl_model_desc* m, int* family, DevProfile* epl, 
         shear->type = p.type;
         for (int k = 0; k < 2; ++k) shear->col[k] = p.col[k];
       } else {
-        set_error("fused model: lens profile type %d is not supported (EPL, SHEAR)", p.type);
-        return GL_ERR_UNSUPPORTED;
+        return false;
       }
-    } else if (p.group == GL_GROUP_LENS_LIGHT || p.group == GL_GROUP_SOURCE) {
+    } else {
       DevProfile* dst = p.group == GL_GROUP_LENS_LIGHT ? llight : source;
       int* cnt = p.group == GL_GROUP_LENS_LIGHT ? &n_ll : &n_src;
       ++*cnt;
       dst->type = GL_PROF_SERSIC_ELLIPSE;
+      if (p.use_lstsq) return false;
       if (p.type == GL_PROF_SERSIC_ELLIPSE) {
         for (int k = 0; k < 7; ++k) dst->col[k] = p.col[k];
       } else if (p.type == GL_PROF_SERSIC) {
@@ -85,27 +88,136 @@ static int resolve_family(const gl_model_desc* m, int* family, DevProfile* epl, 
         dst->col[5] = p.col[3];
         dst->col[6] = p.col[4];
       } else {
-        set_error("fused model: light profile type %d is not supported (SERSIC, SERSIC_ELLIPSE)",
-                  p.type);
+        return false;
+      }
+    }
+  }
+  if (n_epl != 1 || n_shear > 1 || n_ll > 1 || n_src != 1) return false;
+  if (n_shear) *family = n_ll ? FAM_EPL_SHEAR_SE_SE : FAM_EPL_SHEAR_SE;
+  else *family = n_ll ? FAM_EPL_SE_SE : FAM_EPL_SE;
+  return true;
+}
+
+// The model on the fused kernel's general path.  With lsq, light profiles
+// with use_lstsq take their amplitudes from the least-squares coefficient
+// vector, in the channel order of the least-squares planner (light profiles
+// in descriptor order; one channel per Sersic, D per shapelet set).
+static int resolve_generic(const gl_model_desc* m, bool lsq, GenArgs* g, DevProfile* epl,
+                           DevProfile* shear) {
+  memset(g, 0, sizeof(*g));
+  for (auto* p : {epl, shear}) {
+    p->type = GL_PROF_NONE;
+    p->niter = 0;
+    for (int i = 0; i < GL_MAX_PROFILE_PARAMS; ++i) p->col[i] = -1;
+  }
+  int n_amp = 0;
+  for (int i = 0; i < m->n_profiles; ++i) {
+    const gl_profile_desc& p = m->prof[i];
+    if (p.group == GL_GROUP_LENS) {
+      if (p.type == GL_PROF_SHEAR) {
+        if (g->has_shear) {
+          set_error("at most one SHEAR profile");
+          return GL_ERR_UNSUPPORTED;
+        }
+        g->has_shear = 1;
+        shear->type = p.type;
+        for (int k = 0; k < 2; ++k) shear->col[k] = p.col[k];
+        continue;
+      }
+      if (p.type != GL_PROF_EPL && p.type != GL_PROF_SIS && p.type != GL_PROF_SIE &&
+          p.type != GL_PROF_TNFW) {
+        set_error("lens profile type %d is not a mass profile", p.type);
+        return GL_ERR_INVALID;
+      }
+      if (g->n_mass >= kGenMass) {
+        set_error("at most %d mass profiles besides SHEAR", kGenMass);
         return GL_ERR_UNSUPPORTED;
       }
-      if (p.use_lstsq) dst->col[6] = -1;   // unit amplitude
+      DevProfile& d = g->mass[g->n_mass++];
+      d.type = p.type;
+      d.niter = p.niter;
+      for (int k = 0; k < GL_MAX_PROFILE_PARAMS; ++k) d.col[k] = p.col[k];
+      if (p.type == GL_PROF_EPL) {
+        if (epl->type == GL_PROF_EPL) {
+          set_error("at most one EPL profile");
+          return GL_ERR_UNSUPPORTED;
+        }
+        if (p.niter < 0 || p.niter > kMaxTerms) {
+          set_error("EPL niter %d outside [0, %d]", p.niter, kMaxTerms);
+          return GL_ERR_UNSUPPORTED;
+        }
+        *epl = d;
+      }
+    } else if (p.group == GL_GROUP_LENS_LIGHT || p.group == GL_GROUP_SOURCE) {
+      if (g->n_light >= kGenLight) {
+        set_error("at most %d light profiles", kGenLight);
+        return GL_ERR_UNSUPPORTED;
+      }
+      GenLight& L = g->light[g->n_light++];
+      L.group = p.group;
+      for (int k = 0; k < GL_MAX_PROFILE_PARAMS; ++k) L.col[k] = -1;
+      const bool ext = lsq && p.use_lstsq;
+      L.amp_ext = ext ? 1 : 0;
+      L.amp_idx = n_amp;
+      if (p.type == GL_PROF_SERSIC_ELLIPSE || p.type == GL_PROF_SERSIC) {
+        L.type = GL_PROF_SERSIC_ELLIPSE;
+        if (p.type == GL_PROF_SERSIC_ELLIPSE) {
+          for (int k = 0; k < 7; ++k) L.col[k] = p.col[k];
+        } else {
+          L.col[0] = p.col[0];
+          L.col[1] = p.col[1];
+          L.col[4] = p.col[2];
+          L.col[5] = p.col[3];
+          L.col[6] = p.col[4];
+        }
+        if (p.use_lstsq) L.col[6] = -1;   // unit amplitude (or the coefficient)
+        if (ext) n_amp += 1;
+      } else if (p.type == GL_PROF_CORE_SERSIC) {
+        L.type = p.type;
+        for (int k = 0; k < 10; ++k) L.col[k] = p.col[k];
+        if (p.use_lstsq) L.col[9] = -1;
+        if (ext) n_amp += 1;
+      } else if (p.type == GL_PROF_SHAPELETS) {
+        L.type = p.type;
+        if (p.niter < 0 || p.niter > kMaxShapeletN) {
+          set_error("shapelets n_max %d outside [0, %d]", p.niter, kMaxShapeletN);
+          return GL_ERR_UNSUPPORTED;
+        }
+        L.n_max = p.niter;
+        for (int k = 0; k < 3; ++k) L.col[k] = p.col[k];
+        const int D = (p.niter + 1) * (p.niter + 2) / 2;
+        if (ext) {
+          n_amp += D;
+        } else if (p.use_lstsq) {
+          set_error("shapelets with use_lstsq need the least-squares coefficients (gl_lstsq)");
+          return GL_ERR_UNSUPPORTED;
+        } else {
+          if (p.col[3] < 0 || p.col[3] + D > m->n_params) {
+            set_error("shapelets: amplitude columns %d..%d outside the parameter vector", p.col[3],
+                      p.col[3] + D - 1);
+            return GL_ERR_INVALID;
+          }
+          L.col[3] = p.col[3];
+          g->explicit_shapelets = 1;
+        }
+      } else {
+        set_error("light profile type %d is not a light profile", p.type);
+        return GL_ERR_INVALID;
+      }
     } else {
       set_error("profile %d: bad group %d", i, p.group);
       return GL_ERR_INVALID;
     }
   }
-  if (n_epl != 1 || n_shear > 1 || n_ll > 1 || n_src != 1) {
-    set_error("fused model needs one EPL, at most one SHEAR, at most one lens light and one source "
-              "light profile (got %d, %d, %d, %d)", n_epl, n_shear, n_ll, n_src);
+  if (g->n_light < 1) {
+    set_error("the model needs at least one light profile");
+    return GL_ERR_INVALID;
+  }
+  if (n_amp > kMaxAmps) {
+    set_error("%d linear amplitudes exceed %d", n_amp, kMaxAmps);
     return GL_ERR_UNSUPPORTED;
   }
-  if (epl->niter < 0 || epl->niter > kMaxTerms) {
-    set_error("EPL niter %d outside [0, %d]", epl->niter, kMaxTerms);
-    return GL_ERR_UNSUPPORTED;
-  }
-  if (n_shear) *family = n_ll ? FAM_EPL_SHEAR_SE_SE : FAM_EPL_SHEAR_SE;
-  else *family = n_ll ? FAM_EPL_SE_SE : FAM_EPL_SE;
+  g->n_amp = n_amp;
   return GL_OK;
 }
 
@@ -163,17 +275,13 @@ static int build_image(const gl_image_desc& g, DevImage& I, HostImage& hi) {
     set_error("PSF too large for the fused kernel: sub-kernel side %d > %d", KS, kMaxKS);
     return GL_ERR_UNSUPPORTED;
   }
-  if (KS % 2 == 0) {
-    set_error("PSF size %d with supersample %d gives an even sub-kernel (%d); not supported", k, ss,
-              KS);
-    return GL_ERR_UNSUPPORTED;
-  }
   I.KS = KS;
   I.ksp = (KS + 3) & ~3;
   for (int p = 0; p < ss; ++p) I.d[p] = (p + pad) / ss;
   for (int p = 1; p < ss; ++p)
-    if ((I.d[p] - I.d[0]) % 4 != 0) {
-      set_error("PSF size %d with supersample %d: unaligned parity offsets; not supported", k, ss);
+    if (I.d[p] - I.d[0] < 0 || I.d[p] - I.d[0] > 1 || (I.d[p] != I.d[0] && KS % 2)) {
+      set_error("PSF size %d with supersample %d: parity offsets %d, %d not supported", k, ss, I.d[0],
+                I.d[p]);
       return GL_ERR_UNSUPPORTED;
     }
   hi.kern.assign(I.nplanes * KS * I.ksp, 0.f);
@@ -187,10 +295,13 @@ static int build_image(const gl_image_desc& g, DevImage& I, HostImage& hi) {
         }
   // shared-memory layout
   // The pitch covers the segments read by the fused kernel (kFusedCB columns
-  // per unit) and by the least-squares kernel (kColBlock columns per unit).
+  // per unit, plus one when the transposed correlation of column parity 1
+  // starts one float past a 16-byte boundary: PSF sizes k = 3 mod 4 at ss = 2)
+  // and by the least-squares kernel (kColBlock columns per unit).
+  const int max_shift = I.d[ss - 1] - I.d[0];
   I.ncb = ((N + kFusedCB - 1) / kFusedCB + 1) & ~1;
   I.units = N * I.ncb;
-  const int seg_f = (kFusedCB + KS - 1 + 3) & ~3;
+  const int seg_f = (kFusedCB + KS - 1 + max_shift + 3) & ~3;
   const int seg_l = (kColBlock + KS - 1 + 3) & ~3;
   const int ncb_l = (N + kColBlock - 1) / kColBlock;
   int pitch = (int)align_up(std::max(kFusedCB * (I.ncb - 1) + seg_f, kColBlock * (ncb_l - 1) + seg_l), 4);
@@ -303,6 +414,7 @@ static void fill_args(const gl_plan* plan, FusedArgs& a) {
   a.shear = plan->shear;
   a.llight = plan->llight;
   a.source = plan->source;
+  a.gen = plan->gen;
   a.has_prior = plan->has_prior;
   for (int i = 0; i < GL_MAX_PARAMS; ++i) a.prior[i] = plan->prior[i];
   a.img_stride = plan->max_pix;
@@ -361,14 +473,27 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
   // a model whose light is solved linearly runs on the least-squares kernels
   bool lsq_model = false;
   for (int i = 0; i < model->n_profiles; ++i)
-    if (model->prof[i].group != GL_GROUP_LENS &&
-        (model->prof[i].use_lstsq || model->prof[i].type == GL_PROF_SHAPELETS))
-      lsq_model = true;
+    if (model->prof[i].group != GL_GROUP_LENS && model->prof[i].use_lstsq) lsq_model = true;
   int rc = GL_OK;
   if (lsq_model) {
     plan->family = -1;
-  } else {
-    rc = resolve_family(model, &plan->family, &plan->epl, &plan->shear, &plan->llight, &plan->source);
+    // the general path with the coefficients as amplitudes (gl_lstsq_grad)
+    DevProfile e, sh;
+    plan->gen_ok = resolve_generic(model, true, &plan->gen, &e, &sh) == GL_OK;
+    if (plan->gen_ok) {
+      plan->epl = e;
+      plan->shear = sh;
+    }
+    set_error("");
+  } else if (!resolve_family(model, &plan->family, &plan->epl, &plan->shear, &plan->llight,
+                             &plan->source)) {
+    rc = resolve_generic(model, false, &plan->gen, &plan->epl, &plan->shear);
+    plan->family = FAM_GENERIC;
+    plan->gen_ok = rc == GL_OK;
+  }
+  if (!rc && plan->epl.type == GL_PROF_EPL && (plan->epl.niter < 0 || plan->epl.niter > kMaxTerms)) {
+    set_error("EPL niter %d outside [0, %d]", plan->epl.niter, kMaxTerms);
+    rc = GL_ERR_UNSUPPORTED;
   }
   if (rc) {
     delete plan;
@@ -390,7 +515,7 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
       return rc;
     }
     bytes += align_up(hi[i].obs.size() * 4, 256) + align_up(hi[i].grid.size() * 4, 256) +
-             align_up(hi[i].kern.size() * 4, 256);
+             align_up(hi[i].kern.size() * 4, 256) + align_up(hi[i].err.size() * 4, 256);
     if (plan->img[i].smem_floats > smem_floats) smem_floats = plan->img[i].smem_floats;
     const int pix = images[i].num_pix * images[i].num_pix;
     if (pix > plan->max_pix) plan->max_pix = pix;
@@ -399,7 +524,8 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
   plan->smem_bytes = smem_floats * 4;
   const int static_smem = lsq_model ? 0 : fused_static_smem_bytes();
-  if (!lsq_model && plan->smem_bytes + static_smem > dev_smem) {
+  plan->fused_fits = plan->smem_bytes + fused_static_smem_bytes() <= dev_smem;
+  if (!lsq_model && !plan->fused_fits) {
     set_error("image needs %d bytes of shared memory; the device allows %d per block",
               plan->smem_bytes + static_smem, dev_smem);
     delete plan;
@@ -424,9 +550,10 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
     I.obs = put(hi[i].obs);
     I.grid = put(hi[i].grid);
     I.kern = put(hi[i].kern);
+    I.err = put(hi[i].err);
   }
   rc = cuda_check(cudaGetLastError(), "plan upload");
-  if (!rc && !lsq_model) rc = fused_kernel_prepare(plan->smem_bytes);
+  if (!rc && plan->fused_fits) rc = fused_kernel_prepare(plan->smem_bytes);
   if (!rc && lsq_model) {
     std::vector<std::vector<float>> errs(n_images);
     for (int i = 0; i < n_images; ++i) errs[i] = hi[i].err;
@@ -518,6 +645,15 @@ int gl_plan_query(const gl_plan* plan, int* smem_bytes, int* threads_per_block, 
   return GL_OK;
 }
 
+static int grad_checks(const gl_plan* plan) {
+  if (plan->family == FAM_GENERIC && plan->gen.explicit_shapelets) {
+    set_error("gradients with respect to explicit shapelet amplitudes are not implemented; "
+              "use Shapelets(use_lstsq=True)");
+    return GL_ERR_UNSUPPORTED;
+  }
+  return GL_OK;
+}
+
 static int common_checks(const gl_plan* plan, const float* x, int bs) {
   if (!plan || (bs > 0 && !x) || bs < 0) {
     set_error("null plan / input or negative batch");
@@ -555,6 +691,7 @@ int gl_forward(const gl_plan* plan, const float* x, const int* img_id, int bs, f
 int gl_forward_grad(const gl_plan* plan, const float* x, const int* img_id, int bs, float* logL,
                     float* chi2, float* dlogL_dx, int* status, void* stream) {
   int rc = common_checks(plan, x, bs);
+  if (!rc && dlogL_dx) rc = grad_checks(plan);
   if (rc) return rc;
   for (int i = 0; i < plan->n_images; ++i)
     if (!plan->img[i].obs) {
@@ -577,6 +714,7 @@ int gl_forward_grad(const gl_plan* plan, const float* x, const int* img_id, int 
 int gl_adjoint(const gl_plan* plan, const float* x, const int* img_id, int bs, const float* dlogL,
                float* dx, int* status, void* stream) {
   int rc = common_checks(plan, x, bs);
+  if (!rc) rc = grad_checks(plan);
   if (rc) return rc;
   if (!dx || !dlogL) {
     set_error("gl_adjoint: dlogL and dx are required");
@@ -597,6 +735,7 @@ int gl_adjoint(const gl_plan* plan, const float* x, const int* img_id, int bs, c
 int gl_log_prob(const gl_plan* plan, const float* z, const int* img_id, int bs, float* logp,
                 float* chi2, float* dlogp_dz, int* status, void* stream) {
   int rc = common_checks(plan, z, bs);
+  if (!rc && dlogp_dz) rc = grad_checks(plan);
   if (rc) return rc;
   if (!plan->has_prior) {
     set_error("gl_log_prob: the plan has no prior (gl_plan_set_prior)");
@@ -613,6 +752,48 @@ int gl_log_prob(const gl_plan* plan, const float* z, const int* img_id, int bs, 
   a.status = status;
   a.zmode = 1;
   a.want_grad = dlogp_dz != nullptr;
+  return launch_fused(a, plan->smem_bytes, (cudaStream_t)stream);
+}
+
+int gl_lstsq_grad(const gl_plan* plan, const float* x, const int* img_id, int bs,
+                  const float* coeffs, float* logL, float* chi2, float* grad, void* stream) {
+  if (!plan || bs < 0 || (bs > 0 && (!x || !coeffs || !grad))) {
+    set_error("gl_lstsq_grad: null plan, input, coefficients or gradient, or negative batch");
+    return GL_ERR_INVALID;
+  }
+  if (!plan->lsq) {
+    set_error("gl_lstsq_grad: the plan's light profiles are not solved linearly");
+    return GL_ERR_INVALID;
+  }
+  if (!plan->gen_ok || plan->gen.n_amp != ((const LsqPlan*)plan->lsq)->D) {
+    set_error("gl_lstsq_grad: the model is not supported by the fused kernel's general path");
+    return GL_ERR_UNSUPPORTED;
+  }
+  if (!plan->fused_fits) {
+    set_error("gl_lstsq_grad: the image needs %d bytes of shared memory per CTA, more than the "
+              "device allows", plan->smem_bytes + fused_static_smem_bytes());
+    return GL_ERR_UNSUPPORTED;
+  }
+  int rc = check_device(plan);
+  if (rc) return rc;
+  for (int i = 0; i < plan->n_images; ++i)
+    if (!plan->img[i].obs || !plan->img[i].err) {
+      set_error("image %d has no observed data", i);
+      return GL_ERR_INVALID;
+    }
+  FusedArgs a;
+  fill_args(plan, a);
+  a.family = FAM_GENERIC;
+  a.gen.amps = coeffs;
+  a.gen.noise_err = 1;
+  a.gen.unit_cf = 1;
+  a.bs = bs;
+  a.x = x;
+  a.img_id = img_id;
+  a.logL = logL;
+  a.chi2 = chi2;
+  a.grad = grad;
+  a.want_grad = 1;
   return launch_fused(a, plan->smem_bytes, (cudaStream_t)stream);
 }
 
@@ -633,7 +814,7 @@ int gl_profile_eval(int type, const float* x, const float* y, int64_t n, const f
     return GL_ERR_INVALID;
   }
   const bool mass = type == GL_PROF_EPL || type == GL_PROF_SHEAR || type == GL_PROF_SIS ||
-                    type == GL_PROF_SIE;
+                    type == GL_PROF_SIE || type == GL_PROF_TNFW;
   if (mass && !out1) {
     set_error("gl_profile_eval: mass profiles need out1");
     return GL_ERR_INVALID;

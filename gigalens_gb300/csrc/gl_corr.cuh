@@ -44,16 +44,17 @@ __device__ __forceinline__ void corr_row(const float* __restrict__ seg,
   }
 }
 
-// n consecutive rows: acc[c] += sum_r sum_l k_r[l] * seg_r[c + l], with
-// seg_r = seg + r * seg_pitch and k_r = krow + r * k_step (REV: taps reversed).
-// The next row's segment is loaded while the current one is consumed.  The
-// prefetch of row n (one past the last) must stay inside shared memory; its
-// values are not used.
-template <int KS, bool REV, int CB>
+// n consecutive rows: acc[c] += sum_r sum_l k_r[l] * seg_r[c + l + SHIFT],
+// with seg_r = seg + r * seg_pitch (16-byte aligned; SHIFT < 4 skips the
+// first floats of the aligned segment) and k_r = krow + r * k_step (REV: taps
+// reversed).  The next row's segment is loaded while the current one is
+// consumed.  The prefetch of row n (one past the last) must stay inside
+// shared memory; its values are not used.
+template <int KS, bool REV, int CB, int SHIFT = 0>
 __device__ __forceinline__ void corr_rows(const float* __restrict__ seg, int seg_pitch,
                                           const float* __restrict__ krow, int k_step, int n,
                                           float (&acc)[CB]) {
-  constexpr int SEGN = (CB + KS - 1 + 3) & ~3;
+  constexpr int SEGN = (CB + KS - 1 + SHIFT + 3) & ~3;
   constexpr int NG = (KS + 3) / 4;
   float4 cur[SEGN / 4];
 #pragma unroll
@@ -85,7 +86,7 @@ __device__ __forceinline__ void corr_rows(const float* __restrict__ seg, int seg
         if (kidx < KS) {
           const int l = REV ? KS - 1 - kidx : kidx;
 #pragma unroll
-          for (int c = 0; c < CB; ++c) acc[c] = fmaf(kq[e], s[c + l], acc[c]);
+          for (int c = 0; c < CB; ++c) acc[c] = fmaf(kq[e], s[c + l + SHIFT], acc[c]);
         }
       }
     }
@@ -94,21 +95,35 @@ __device__ __forceinline__ void corr_rows(const float* __restrict__ seg, int seg
   }
 }
 
+// Sub-kernel sides 1..25: odd for every PSF at ss = 1 and for PSF sizes
+// k = 1 mod 4 at ss = 2, even for k = 3 mod 4 at ss = 2.
 #define GL_KS_DISPATCH(KSVAL, CALL) \
   switch (KSVAL) {                  \
-    case 1: CALL(1); break;         \
-    case 3: CALL(3); break;         \
-    case 5: CALL(5); break;         \
-    case 7: CALL(7); break;         \
-    case 9: CALL(9); break;         \
-    case 11: CALL(11); break;       \
-    case 13: CALL(13); break;       \
-    case 15: CALL(15); break;       \
-    case 17: CALL(17); break;       \
-    case 19: CALL(19); break;       \
-    case 21: CALL(21); break;       \
-    case 23: CALL(23); break;       \
-    case 25: CALL(25); break;       \
+    case 1: CALL(1); break; \
+    case 2: CALL(2); break; \
+    case 3: CALL(3); break; \
+    case 4: CALL(4); break; \
+    case 5: CALL(5); break; \
+    case 6: CALL(6); break; \
+    case 7: CALL(7); break; \
+    case 8: CALL(8); break; \
+    case 9: CALL(9); break; \
+    case 10: CALL(10); break; \
+    case 11: CALL(11); break; \
+    case 12: CALL(12); break; \
+    case 13: CALL(13); break; \
+    case 14: CALL(14); break; \
+    case 15: CALL(15); break; \
+    case 16: CALL(16); break; \
+    case 17: CALL(17); break; \
+    case 18: CALL(18); break; \
+    case 19: CALL(19); break; \
+    case 20: CALL(20); break; \
+    case 21: CALL(21); break; \
+    case 22: CALL(22); break; \
+    case 23: CALL(23); break; \
+    case 24: CALL(24); break; \
+    case 25: CALL(25); break; \
     default: break;                 \
   }
 

@@ -1,0 +1,8 @@
+// Fused kernel, family FAM_EPL_SE (one translation unit per family).
+#include "gl_fused.cuh"
+
+namespace gl {
+template int fam_launch<FAM_EPL_SE>(const FusedArgs&, int, int, cudaStream_t);
+template cudaError_t fam_set_smem<FAM_EPL_SE>(int);
+template int fam_static_smem<FAM_EPL_SE>();
+}  // namespace gl

@@ -15,6 +15,10 @@ constexpr int kMaxTerms = 256;       // largest EPL iteration cap the fused kern
 constexpr int kMaxKS = 25;           // largest parity sub-kernel side
 constexpr int kMaxPlanes = 4;        // supersample <= 2 in the fused kernel
 constexpr int kRedSlots = 48;        // reduced quantities per sample
+constexpr int kMaxShapeletN = 9;     // shapelets n_max <= 9: at most 55 basis functions
+constexpr int kGenMass = 2;          // general path: mass profiles besides SHEAR
+constexpr int kGenLight = 3;         // general path: light profiles
+constexpr int kMaxAmps = 64;         // general path: external amplitudes per sample
 
 // Per-image constants, in device-ready form.
 struct DevImage {
@@ -38,6 +42,7 @@ struct DevImage {
   const float* grid;// device [nplanes][N][N] float4: (x, y, shared-memory offset of the pixel
                     // in the fused kernel's parity planes as int bits, 0), plane order
   const float* kern;// device [nplanes][KS][ksp] forward parity sub-kernels
+  const float* err; // device N*N noise sigma (data-noise likelihood), or null
   // shared-memory layout (float offsets)
   int offI, offW, offK, smem_floats;
 };
@@ -63,7 +68,32 @@ enum ModelFamily : int {
   FAM_EPL_SHEAR_SE = 1,     // EPL + Shear ; no lens light            ; SersicEllipse source
   FAM_EPL_SE_SE = 2,        // EPL         ; SersicEllipse            ; SersicEllipse
   FAM_EPL_SE = 3,           // EPL         ; no lens light            ; SersicEllipse
-  FAM_COUNT = 4
+  FAM_GENERIC = 4,          // general path: the profile lists of GenArgs, dispatched per pixel
+  FAM_COUNT = 5
+};
+
+// A light profile of the general path.
+struct GenLight {
+  int type;     // GL_PROF_SERSIC_ELLIPSE (SERSIC as e1 = e2 = 0), GL_PROF_CORE_SERSIC, GL_PROF_SHAPELETS
+  int group;    // GL_GROUP_LENS_LIGHT (evaluated at theta) or GL_GROUP_SOURCE (at beta)
+  int n_max;    // shapelets
+  int amp_ext;  // amplitude(s) from the external per-sample vector (least-squares coefficients)
+  int amp_idx;  // index of the (first) amplitude in that vector
+  int col[GL_MAX_PROFILE_PARAMS];   // SERSIC_ELLIPSE / CORE_SERSIC / SHAPELETS canonical columns
+};
+
+// Model of the general path.
+struct GenArgs {
+  int n_mass;
+  DevProfile mass[kGenMass];   // EPL (at most one), SIS, SIE, TNFW
+  int has_shear;
+  int n_light;
+  GenLight light[kGenLight];
+  int n_amp;                   // external amplitudes per sample
+  const float* amps;           // [bs, n_amp] or null
+  int noise_err;               // data-noise likelihood with the image's error map
+  int unit_cf;                 // images without the conversion factor (least-squares images)
+  int explicit_shapelets;      // a shapelet profile with amplitude parameters (no gradient)
 };
 
 struct FusedArgs {
@@ -74,6 +104,7 @@ struct FusedArgs {
   DevImage img[GL_MAX_IMAGES];
   // slots of the compile-time family, resolved to columns
   DevProfile epl, shear, llight, source;
+  GenArgs gen;              // FAM_GENERIC
   int has_prior;
   DevPriorLeaf prior[GL_MAX_PARAMS];
   // inputs / outputs
@@ -106,6 +137,9 @@ struct gl_plan {
   int has_prior;
   gl::DevPriorLeaf prior[GL_MAX_PARAMS];
   gl::DevProfile epl, shear, llight, source;
+  gl::GenArgs gen;          // the model on the fused kernel's general path
+  int gen_ok;               // gen describes the model
+  int fused_fits;           // the images fit the fused kernel's shared memory
   void* lsq;                // gl::LsqPlan of the least-squares path, or null
 };
 

@@ -243,11 +243,11 @@ __global__ void __launch_bounds__(256) lsq_gram_kernel(const __grid_constant__ L
     const float* Xb = a.X + (size_t)b * a.xstride;
     // entries e = tid + k*256 of the upper triangle (then h): decode (i, j) once
     constexpr int kMaxE = (kMaxLsqChannels * (kMaxLsqChannels + 1) / 2 + kMaxLsqChannels + 255) / 256;
-    float accv[kMaxE];
+    double accv[kMaxE];   // 32-pixel partial sums in float32, accumulated in float64
     int ei[kMaxE], ej[kMaxE];
 #pragma unroll
     for (int k = 0; k < kMaxE; ++k) {
-      accv[k] = 0.f;
+      accv[k] = 0.0;
       const int e = threadIdx.x + 256 * k;
       int i = -1, j = -1;
       if (e < ntri) {
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(256) lsq_gram_kernel(const __grid_constant__ L
         float s = 0.f;
 #pragma unroll 8
         for (int pp = 0; pp < 32; ++pp) s = fmaf(xs[i][pp], xj[pp], s);
-        accv[k] += s;
+        accv[k] += (double)s;
       }
     }
 #pragma unroll
@@ -296,10 +296,10 @@ __global__ void __launch_bounds__(256) lsq_gram_kernel(const __grid_constant__ L
       const int i = ei[k], j = ej[k];
       if (i < 0) continue;
       if (j >= 0) {
-        G[((size_t)b * D + i) * D + j] = accv[k];
-        G[((size_t)b * D + j) * D + i] = accv[k];
+        G[((size_t)b * D + i) * D + j] = (float)accv[k];
+        G[((size_t)b * D + j) * D + i] = (float)accv[k];
       } else {
-        h[(size_t)b * D + i] = accv[k];
+        h[(size_t)b * D + i] = (float)accv[k];
       }
     }
   }
@@ -423,11 +423,42 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
       proj[i] = (i < D && fabsf(lam) > cutoff) ? s / lam : 0.f;
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < D; r += blockDim.x) {
+    __shared__ float cvec[kMaxLsqChannels + 1];
+    __shared__ float rvec[kMaxLsqChannels + 1];
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
       float s = 0.f;
       for (int i = 0; i < n; ++i) s = fmaf(V[r][i], proj[i], s);
-      coeffs[(size_t)b * D + r] = s;
+      cvec[r] = r < D ? s : 0.f;
     }
+    __syncthreads();
+    // Iterative refinement against the float32 normal equations: the residual
+    // r = h - G c is accumulated in float64 and its pinv image added to c.  It
+    // removes the error of the float32 eigen-solve, to which the likelihood
+    // gradient at the solution is first-order sensitive.
+    const float* Gb = G + (size_t)b * D * D;
+    for (int it = 0; it < 2; ++it) {
+      for (int row = threadIdx.x; row < n; row += blockDim.x) {
+        double acc = row < D ? (double)hs[row] : 0.0;
+        if (row < D)
+          for (int j = 0; j < D; ++j) acc -= (double)Gb[(size_t)row * D + j] * (double)cvec[j];
+        rvec[row] = (float)acc;
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        float s = 0.f;
+        for (int r = 0; r < n; ++r) s = fmaf(V[r][i], rvec[r], s);
+        const float lam = A[i][i];
+        proj[i] = (i < D && fabsf(lam) > cutoff) ? s / lam : 0.f;
+      }
+      __syncthreads();
+      for (int r = threadIdx.x; r < D; r += blockDim.x) {
+        float s = 0.f;
+        for (int i = 0; i < n; ++i) s = fmaf(V[r][i], proj[i], s);
+        cvec[r] += s;
+      }
+      __syncthreads();
+    }
+    for (int r = threadIdx.x; r < D; r += blockDim.x) coeffs[(size_t)b * D + r] = cvec[r];
     __syncthreads();
   }
 }

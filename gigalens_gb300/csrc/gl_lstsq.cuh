@@ -9,7 +9,6 @@ namespace gl {
 
 constexpr int kMaxLsqChannels = 64;   // basis images per sample (shapelets n_max <= 9 + lens light)
 constexpr int kMaxLsqProfiles = 4;
-constexpr int kMaxShapeletN = 9;
 
 struct LsqChannel {
   int kind;    // 0: unit-amplitude Sersic, 1: shapelet basis function

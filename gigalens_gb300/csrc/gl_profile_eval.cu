@@ -4,6 +4,7 @@
 // the same arithmetic from gl_profiles.cuh.
 #include "gl_internal.cuh"
 #include "gl_profiles.cuh"
+#include "gl_profiles_gen.cuh"
 
 namespace gl {
 
@@ -41,14 +42,21 @@ __global__ void profile_eval_kernel(const float* __restrict__ x, const float* __
       out1[i] = g2 * xi - g1 * yi;
     } else if (TYPE == GL_PROF_SIS) {
       float ax, ay;
-      sis_deflect(P(0), P(1), P(2), xi, yi, ax, ay);
+      sis_alpha_t<float>(P(0), P(1), P(2), xi, yi, ax, ay);
       out0[i] = ax;
       out1[i] = ay;
     } else if (TYPE == GL_PROF_SIE) {
       float ax, ay;
-      sie_deflect(P(0), P(1), P(2), P(3), P(4), xi, yi, ax, ay);
+      sie_alpha_t<float>(P(0), P(1), P(2), P(3), P(4), xi, yi, ax, ay);
       out0[i] = ax;
       out1[i] = ay;
+    } else if (TYPE == GL_PROF_TNFW) {
+      float ax, ay;
+      tnfw_alpha_t<float>(P(0), P(1), P(2), P(3), P(4), xi, yi, ax, ay);
+      out0[i] = ax;
+      out1[i] = ay;
+    } else if (TYPE == GL_PROF_CORE_SERSIC) {
+      out0[i] = P(9) * core_sersic_t<float>(P(0), P(1), P(2), P(3), P(4), P(5), P(6), P(7), P(8), xi, yi);
     } else if (TYPE == GL_PROF_SERSIC) {
       SerC s = sersic_consts(P(0), P(1), 0.f, 0.f, P(2), P(3), P(4));
       out0[i] = sersic_light(s, xi, yi);
@@ -75,6 +83,8 @@ int launch_profile_eval(int type, const float* x, const float* y, int64_t n, con
     GL_CASE(GL_PROF_SHEAR)
     GL_CASE(GL_PROF_SIS)
     GL_CASE(GL_PROF_SIE)
+    GL_CASE(GL_PROF_TNFW)
+    GL_CASE(GL_PROF_CORE_SERSIC)
     GL_CASE(GL_PROF_SERSIC)
     GL_CASE(GL_PROF_SERSIC_ELLIPSE)
 #undef GL_CASE

@@ -4,8 +4,6 @@
 // Forward formulas follow the reference:
 //   EPL    gigalens/tf/profiles/mass/epl.py:23-68  (Tessore-Metcalf series)
 //   Shear  gigalens/tf/profiles/mass/shear.py:12-14
-//   SIS    gigalens/tf/profiles/mass/sis.py:13-18
-//   SIE    gigalens/tf/profiles/mass/sie.py:14-43
 //   Sersic gigalens/tf/profiles/light/sersic.py:25-72
 // The reverse mode is written by hand: it replaces TensorFlow autodiff and
 // differentiates the same expressions.  The EPL series is not stored: its
@@ -451,35 +449,6 @@ __device__ __forceinline__ void sersic_chain(float Rs, float n, float e1, float 
   out[4] = a.cx;
   out[5] = a.cy;
   out[6] = a.Ie;
-}
-
-// ------------------------------------------------------------------ SIS / SIE
-__device__ __forceinline__ void sis_deflect(float theta_E, float cx, float cy, float x, float y,
-                                            float& ax, float& ay) {
-  float dx = x - cx, dy = y - cy;
-  float R = sqrtf(dx * dx + dy * dy);
-  float a = (R == 0.f) ? 0.f : theta_E / R;
-  ax = a * dx;
-  ay = a * dy;
-}
-
-__device__ __forceinline__ void sie_deflect(float theta_E, float e1, float e2, float cx, float cy,
-                                            float x, float y, float& ax, float& ay) {
-  float phi = atan2f(e2, e1) * 0.5f;
-  float c = fminf(sqrtf(e1 * e1 + e2 * e2), 0.9999f);
-  float q = (1.f - c) / (1.f + c);
-  float theta_E_conv = theta_E / sqrtf((1.f + q * q) / (2.f * q));
-  float b = theta_E_conv * sqrtf((1.f + q * q) / 2.f);
-  float sp, cp;
-  sincosf(phi, &sp, &cp);
-  float dx = x - cx, dy = y - cy;
-  float xr = dx * cp + dy * sp, yr = -dx * sp + dy * cp;
-  float psi = sqrtf(q * q * (xr * xr) + yr * yr);
-  float sq = sqrtf(1.f - q * q);
-  float fx = b / sq * atanf(sq * xr / psi);
-  float fy = b / sq * atanhf(sq * yr / psi);
-  ax = fx * cp - fy * sp;
-  ay = fx * sp + fy * cp;
 }
 
 }  // namespace gl

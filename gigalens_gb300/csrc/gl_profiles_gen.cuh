@@ -1,0 +1,188 @@
+// Closed-form profiles of the fused kernel's general path and of the
+// elementwise profile kernels, each written once as a template over its
+// scalar type: float gives the value, Dual<N> the value and its derivatives
+// (see gl_dual.cuh).  Formulas follow the reference:
+//   SIS         gigalens/tf/profiles/mass/sis.py:13-18
+//   SIE         gigalens/tf/profiles/mass/sie.py:14-43 (s_scale = 0)
+//   TNFW        gigalens/tf/profiles/mass/tnfw.py:14-58
+//   CoreSersic  gigalens/tf/profiles/light/sersic.py:88-121, with the
+//               reference's grouping kept as it is: the core term
+//               (1 + (Rb/R)^alpha)^(gamma/alpha) times
+//               exp(-bn ((R^alpha + Rb^alpha) / R_sersic^alpha / (alpha n)) - 1)
+//   Shapelets   gigalens/tf/profiles/light/shapelets.py:66-85 (interpolate=False)
+#pragma once
+#include "gl_dual.cuh"
+
+namespace gl {
+
+constexpr float kPiF = 3.14159265358979f;
+
+// sqrt with a zero derivative at 0 (the reference's sqrt gradient is infinite
+// there; the profiles below only take sqrt(0) where the result is not used
+// through its derivative, e.g. e1 = e2 = 0).
+__device__ __forceinline__ float gsqrt0(float x) { return sqrtf(x); }
+template <int N>
+__device__ __forceinline__ Dual<N> gsqrt0(const Dual<N>& x) {
+  const float s = sqrtf(x.v);
+  return chain1(x, s, s > 0.f ? 0.5f / s : 0.f);
+}
+
+// ------------------------------------------------------------------ SIS
+template <class T>
+__device__ __forceinline__ void sis_alpha_t(const T& theta_E, const T& cx, const T& cy, float x,
+                                            float y, T& ax, T& ay) {
+  const T dx = x - cx, dy = y - cy;
+  const T R = gsqrt0(dx * dx + dy * dy);
+  const T a = (val(R) == 0.f) ? T(0.f) : theta_E / R;
+  ax = a * dx;
+  ay = a * dy;
+}
+
+// ------------------------------------------------------------------ SIE
+template <class T>
+__device__ __forceinline__ void sie_alpha_t(const T& theta_E, const T& e1, const T& e2, const T& cx,
+                                            const T& cy, float x, float y, T& ax, T& ay) {
+  const T phi = gatan2(e2, e1) * 0.5f;
+  T c = gsqrt0(e1 * e1 + e2 * e2);
+  if (val(c) > 0.9999f) c = T(0.9999f);   // tf.math.minimum(c, 0.9999)
+  const T q = (1.f - c) / (1.f + c);
+  const T q2 = q * q;
+  const T theta_E_conv = theta_E / gsqrt((1.f + q2) / (2.f * q));
+  const T b = theta_E_conv * gsqrt((1.f + q2) / 2.f);
+  const T cp = gcos(phi), sp = gsin(phi);
+  const T dx = x - cx, dy = y - cy;
+  const T xr = dx * cp + dy * sp;
+  const T yr = -dx * sp + dy * cp;
+  const T psi = gsqrt(q2 * (xr * xr) + yr * yr);
+  const T sq = gsqrt(1.f - q2);
+  const T fx = b / sq * gatan(sq * xr / psi);
+  const T fy = b / sq * gatanh(sq * yr / psi);
+  ax = fx * cp - fy * sp;
+  ay = fx * sp + fy * cp;
+}
+
+// ------------------------------------------------------------------ TNFW
+// F(x) of the NFW profile, tnfw.py:41-58 (exactly 1 at x == 1)
+template <class T>
+__device__ __forceinline__ T tnfw_F(const T& X) {
+  const float xv = val(X);
+  if (xv < 1.f) {
+    const T s = gsqrt(1.f - X * X);
+    return gatanh(s) / s;
+  }
+  if (xv > 1.f) {
+    const T s = gsqrt(X * X - 1.f);
+    return gatan(s) / s;
+  }
+  return T(1.f);
+}
+
+template <class T>
+__device__ __forceinline__ void tnfw_alpha_t(const T& Rs, const T& alpha_Rs, const T& r_trunc,
+                                             const T& cx, const T& cy, float x, float y, T& ax,
+                                             T& ay) {
+  const T rho0 = alpha_Rs / (4.f * (Rs * Rs) * (1.f + logf(0.5f)));
+  const T dx = x - cx, dy = y - cy;
+  T R = gsqrt0(dx * dx + dy * dy);
+  const T Rmin = 0.001f * Rs;
+  if (!(val(R) >= val(Rmin))) R = Rmin;   // tf.maximum(R, 0.001 Rs)
+  const T X = R / Rs;
+  const T tau = r_trunc / Rs;
+  const T t2 = tau * tau;
+  const T st = gsqrt(t2 + X * X);
+  const T L = glog(X / (tau + st));
+  const T F = tnfw_F(X);
+  const T t21 = t2 + 1.f;
+  const T gx = t2 / (t21 * t21) *
+               ((t21 + 2.f * (X * X - 1.f)) * F + tau * kPiF + (t2 - 1.f) * glog(tau) +
+                st * (-kPiF + L * (t2 - 1.f) / tau));
+  const T a = 4.f * rho0 * Rs * gx / (X * X);
+  ax = a * dx;
+  ay = a * dy;
+}
+
+// ------------------------------------------------------------------ CoreSersic
+// Sersic distance, tf/profiles/light/sersic.py:33-59
+template <class T>
+__device__ __forceinline__ T sersic_distance_t(const T& X, const T& Y, const T& cx, const T& cy,
+                                               const T& e1, const T& e2) {
+  const T phi = gatan2(e2, e1) * 0.5f;
+  const T c = gsqrt0(e1 * e1 + e2 * e2);
+  const T q = (1.f - c) / (1.f + c);
+  const T dx = X - cx, dy = Y - cy;
+  const T cp = gcos(phi), sp = gsin(phi);
+  const T sq = gsqrt(q);
+  const T xt1 = (cp * dx + sp * dy) * sq;
+  const T xt2 = (-sp * dx + cp * dy) / sq;
+  return gsqrt0(xt1 * xt1 + xt2 * xt2);
+}
+
+// unit-amplitude CoreSersic (the caller multiplies by Ie)
+template <class T>
+__device__ __forceinline__ T core_sersic_t(const T& Rs, const T& n, const T& Rb, const T& alpha,
+                                           const T& gamma, const T& e1, const T& e2, const T& cx,
+                                           const T& cy, const T& X, const T& Y) {
+  const T R = sersic_distance_t(X, Y, cx, cy, e1, e2);
+  const T bn = 1.9992f * n - 0.3271f;
+  const T core = gpow(1.f + gpow(Rb / R, alpha), gamma / alpha);
+  const T arg = -bn * ((gpow(R, alpha) + gpow(Rb, alpha)) / gpow(Rs, alpha) / (alpha * n)) - 1.f;
+  return core * gexp(arg);
+}
+
+// ------------------------------------------------------------------ Shapelets
+// phi_n(t) = H_n(t) / sqrt(2^n sqrt(pi) n!) for n = 0..nmax (physicists'
+// Hermite polynomials, H_n = 2 (t H_{n-1} - (n-1) H_{n-2})).
+__device__ __forceinline__ void shapelet_phis(float t, int nmax, const float* pref,
+                                              float (&ph)[kMaxShapeletN + 1]) {
+  float h0 = 1.f, h1 = 2.f * t;
+  ph[0] = pref[0];
+#pragma unroll
+  for (int k = 1; k <= kMaxShapeletN; ++k) {
+    if (k <= nmax) {
+      if (k >= 2) {
+        const float h2 = 2.f * (t * h1 - (float)(k - 1) * h0);
+        h0 = h1;
+        h1 = h2;
+      }
+      ph[k] = h1 * pref[k];
+    } else {
+      ph[k] = 0.f;
+    }
+  }
+}
+
+// Value of sum_k amp_k e^{-(u^2+v^2)/2} phi_n1(u) phi_n2(v) (k in the
+// reference's order (0,0), (1,0), (0,1), (2,0), ...), and its u, v partials.
+__device__ __forceinline__ float shapelets_sum(float u, float v, int nmax, const float* amp,
+                                               const float* pref, float* du, float* dv) {
+  float pu[kMaxShapeletN + 1], pv[kMaxShapeletN + 1];
+  shapelet_phis(u, nmax, pref, pu);
+  shapelet_phis(v, nmax, pref, pv);
+  const float fac = expf(-(u * u + v * v) / 2.f);
+  float s = 0.f, su = 0.f, sv = 0.f;
+#pragma unroll
+  for (int m = 0; m <= kMaxShapeletN; ++m) {
+    if (m <= nmax) {
+#pragma unroll
+      for (int j = 0; j <= m; ++j) {
+        const int n1 = m - j, n2 = j;
+        const float c = amp[m * (m + 1) / 2 + j];
+        s = fmaf(c, pu[n1] * pv[n2], s);
+        if (du) {
+          // d/dt phi_n = sqrt(2n) phi_{n-1}
+          const float dpu = n1 > 0 ? sqrtf(2.f * n1) * pu[n1 - 1] : 0.f;
+          const float dpv = n2 > 0 ? sqrtf(2.f * n2) * pv[n2 - 1] : 0.f;
+          su = fmaf(c, dpu * pv[n2], su);
+          sv = fmaf(c, pu[n1] * dpv, sv);
+        }
+      }
+    }
+  }
+  if (du) {
+    *du = fac * (su - u * s);
+    *dv = fac * (sv - v * s);
+  }
+  return fac * s;
+}
+
+}  // namespace gl

@@ -71,6 +71,12 @@ class ModelLayout:
                     pd.col[i] = -1
                 for i, name in enumerate(N.CANONICAL_PARAMS[kind]):
                     pd.col[i] = cols.get(name, -1)
+                if kind == "SHAPELETS" and not prof.use_lstsq:
+                    # explicit amplitudes: consecutive columns (amp00, amp01, .. sort in order)
+                    amp_cols = [cols[k] for k in prof._amp_names]
+                    if amp_cols != list(range(amp_cols[0], amp_cols[0] + len(amp_cols))):
+                        raise ValueError("shapelet amplitude columns are not consecutive")
+                    pd.col[3] = amp_cols[0]
                 n_prof += 1
         desc.n_profiles = n_prof
         desc.n_params = len(self.entries)

@@ -74,7 +74,9 @@ class ForwardProbModel(_model.ProbabilisticModel):
 
 
 class _LstsqLogL(torch.autograd.Function):
-    """Likelihood of the least-squares image: value by ``gl_lstsq``."""
+    """Likelihood of the least-squares image: value by ``gl_lstsq``, gradient by
+    ``gl_lstsq_grad`` (the coefficients minimise chi^2 for the fixed noise map,
+    so the derivative through them vanishes)."""
 
     @staticmethod
     def forward(ctx, x, simulator, plan):

@@ -28,7 +28,7 @@ def evaluate(kind, x, y, params, niter=0):
     n = xs.numel()
     prm = torch.stack([t.expand(shape).reshape(-1) for t in tensors[2:]], dim=0).contiguous()
     out0 = torch.empty(n, dtype=torch.float32, device=dev)
-    mass = kind in ("EPL", "SHEAR", "SIS", "SIE")
+    mass = kind in ("EPL", "SHEAR", "SIS", "SIE", "TNFW")
     out1 = torch.empty(n, dtype=torch.float32, device=dev) if mass else None
     kt = None
     stream = N.stream_ptr()

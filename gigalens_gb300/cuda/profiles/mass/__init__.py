@@ -1,1 +1,1 @@
-from . import epl, shear, sie, sis  # noqa: F401
+from . import epl, shear, sie, sis, tnfw  # noqa: F401

@@ -98,6 +98,16 @@ class LensSimulator(_sim.LensSimulatorInterface):
                N.ptr(logL), N.ptr(chi2), N.stream_ptr())
         return dict(coeffs=coeffs, img=img, logL=logL, chi2=chi2, work=work, D=D.value)
 
+    def lstsq_loglik_grad(self, plan: Plan, x: torch.Tensor, coeffs: torch.Tensor) -> torch.Tensor:
+        """d logL / dx of the least-squares likelihood (data-based noise) at the
+        coefficients ``gl_lstsq`` returned for ``x`` (``gl_lstsq_grad``)."""
+        x = x.to(torch.float32).contiguous()
+        coeffs = coeffs.to(torch.float32).contiguous()
+        grad = torch.empty_like(x)
+        N.call("gl_lstsq_grad", plan.handle, N.ptr(x), None, x.shape[0], N.ptr(coeffs), None, None, N.ptr(grad),
+               N.stream_ptr())
+        return grad
+
     def lstsq_simulate(self, params, observed_image, err_map, return_stacked=False, return_coeffs=False,
                        no_deflection=False):
         """``tf/simulator.py:99-165``: images with the linear amplitudes solved by

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GL_ABI_VERSION 1
+#define GL_ABI_VERSION 2
 
 /* ---- error codes ---------------------------------------------------- */
 #define GL_OK 0
@@ -47,16 +47,18 @@ extern "C" {
 #define GL_PROF_SHEAR 2          /* tf/profiles/mass/shear.py:6  Shear      */
 #define GL_PROF_SIS 3            /* tf/profiles/mass/sis.py:9    SIS        */
 #define GL_PROF_SIE 4            /* tf/profiles/mass/sie.py:9    SIE        */
+#define GL_PROF_TNFW 5           /* tf/profiles/mass/tnfw.py:10  TNFW       */
 #define GL_PROF_SERSIC 10        /* tf/profiles/light/sersic.py:9   Sersic        */
 #define GL_PROF_SERSIC_ELLIPSE 11 /* tf/profiles/light/sersic.py:62 SersicEllipse */
 #define GL_PROF_SHAPELETS 12     /* tf/profiles/light/shapelets.py:11 Shapelets */
+#define GL_PROF_CORE_SERSIC 13   /* tf/profiles/light/sersic.py:75 CoreSersic    */
 
 #define GL_GROUP_LENS 0
 #define GL_GROUP_LENS_LIGHT 1
 #define GL_GROUP_SOURCE 2
 
 #define GL_MAX_PROFILES 8
-#define GL_MAX_PROFILE_PARAMS 8
+#define GL_MAX_PROFILE_PARAMS 12
 #define GL_MAX_IMAGES 8
 #define GL_MAX_PARAMS 64
 
@@ -65,10 +67,22 @@ extern "C" {
  *   SHEAR:          gamma1, gamma2
  *   SIS:            theta_E, center_x, center_y
  *   SIE:            theta_E, e1, e2, center_x, center_y
+ *   TNFW:           Rs, alpha_Rs, r_trunc, center_x, center_y
  *   SERSIC:         R_sersic, n_sersic, center_x, center_y, Ie
  *   SERSIC_ELLIPSE: R_sersic, n_sersic, e1, e2, center_x, center_y, Ie
- *   SHAPELETS:      beta, center_x, center_y
- * A light profile with use_lstsq has no Ie column (col = -1).            */
+ *   CORE_SERSIC:    R_sersic, n_sersic, Rb, alpha, gamma, e1, e2, center_x,
+ *                   center_y, Ie
+ *   SHAPELETS:      beta, center_x, center_y, amp0 (column of the first of
+ *                   the D = (n_max+1)(n_max+2)/2 amplitudes, which are
+ *                   consecutive in the reference's ordering amp00, amp01, ..)
+ * A light profile with use_lstsq has no Ie / amplitude column (col = -1).
+ *
+ * The fused kernel has compiled fast paths for EPL [+ SHEAR] with
+ * SERSIC / SERSIC_ELLIPSE lens light and source; every other model with at
+ * most 2 mass profiles besides SHEAR (at most one EPL), at most one SHEAR
+ * and at most 3 light profiles runs on its general path.  Gradients with
+ * respect to explicit shapelet amplitudes are not computed there
+ * (GL_ERR_UNSUPPORTED): shapelets take part in gradients with use_lstsq.   */
 typedef struct {
   int type;                        /* GL_PROF_*                            */
   int group;                       /* GL_GROUP_*                           */
@@ -173,7 +187,8 @@ int gl_bijector_forward(const gl_plan* plan, const float* z, int bs, float* x, v
 /* Evaluate one profile at n points.  params: [n_params_of_type, n] device
  * (row p = canonical parameter p, one value per point).  EPL uses n_terms
  * series iterations; gl_epl_term_count computes the reference's rule.
- * MassProfile.deriv -> (out0, out1) = deflection; LightProfile.light -> out0.
+ * MassProfile.deriv -> (out0, out1) = deflection; LightProfile.light -> out0
+ * (SERSIC, SERSIC_ELLIPSE, CORE_SERSIC rows include Ie as the last row).
  * (tf/profiles/mass/*.py deriv, tf/profiles/light/sersic.py light.)        */
 int gl_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,
                     const int* n_terms, float* out0, float* out1, void* stream);
@@ -220,6 +235,17 @@ int gl_lstsq(const gl_plan* plan, const float* x, const int* img_id, int bs, voi
  *    threads) race on the array: serialise them.                          */
 int gl_lstsq_noalloc(const gl_plan* plan, const float* x, const int* img_id, int bs,
                      float* coeffs, float* img_out, float* logL, float* chi2, void* stream);
+
+/* Gradient of the BackwardProbModel likelihood (tf/model.py:152-158: the
+ * least-squares image scored with the data-based error map) with respect to
+ * the nonlinear parameters x, at the coefficients gl_lstsq returned for the
+ * same x.  The coefficients minimise chi^2 for the fixed noise map, so by the
+ * envelope theorem d logL/dx = (partial d logL/dx at fixed coefficients);
+ * TensorFlow's derivative through pinv reduces to the same value where the
+ * normal equations are solved exactly.  logL [bs], chi2 [bs] (may be NULL)
+ * are recomputed from the same image; grad [bs, d] is written.            */
+int gl_lstsq_grad(const gl_plan* plan, const float* x, const int* img_id, int bs,
+                  const float* coeffs, float* logL, float* chi2, float* grad, void* stream);
 
 /* ---- optimizer step (graph-capturable) ------------------------------- */
 /* Keras Adam as used by ModellingSequence.MAP (tf/inference.py:34,

@@ -136,6 +136,35 @@ def sie_deriv(x, y, theta_E, e1, e2, center_x, center_y):
     return _rotate(fx, fy, -phi)
 
 
+def tnfw_F(x):
+    """NFW F(x), ``tf/profiles/mass/tnfw.py:40-58``: atanh branch below 1, atan
+    branch above, exactly 1 at x == 1 (each branch evaluated only where taken,
+    as the reference's gather/scatter does)."""
+    lo, hi = x < 1, x > 1
+    x_lo = torch.where(lo, x, torch.full_like(x, 0.5))
+    x_hi = torch.where(hi, x, torch.full_like(x, 2.0))
+    s_lo = torch.sqrt(1 - x_lo ** 2)
+    s_hi = torch.sqrt(x_hi ** 2 - 1)
+    return torch.where(lo, torch.atanh(s_lo) / s_lo, torch.where(hi, torch.atan(s_hi) / s_hi, torch.ones_like(x)))
+
+
+def tnfw_deriv(x, y, Rs, alpha_Rs, r_trunc, center_x, center_y):
+    """``tf/profiles/mass/tnfw.py:14-38``."""
+    rho0 = alpha_Rs / (4.0 * Rs ** 2 * (1.0 + math.log(0.5)))
+    dx, dy = x - center_x, y - center_y
+    R = torch.sqrt(dx ** 2 + dy ** 2)
+    R = torch.maximum(R, 0.001 * Rs)
+    X = R / Rs
+    tau = r_trunc / Rs
+    L = torch.log(X / (tau + torch.sqrt(tau ** 2 + X ** 2)))
+    F = tnfw_F(X)
+    gx = (tau ** 2 / (tau ** 2 + 1) ** 2
+          * ((tau ** 2 + 1 + 2 * (X ** 2 - 1)) * F + tau * math.pi + (tau ** 2 - 1) * torch.log(tau)
+             + torch.sqrt(tau ** 2 + X ** 2) * (-math.pi + L * (tau ** 2 - 1) / tau)))
+    a = 4 * rho0 * Rs * gx / X ** 2
+    return a * dx, a * dy
+
+
 # --------------------------------------------------------------------------
 # light profiles
 # --------------------------------------------------------------------------
@@ -167,6 +196,17 @@ def sersic_light(x, y, R_sersic, n_sersic, center_x, center_y, Ie):
     R = sersic_distance(x, y, center_x, center_y)
     bn = 1.9992 * n_sersic - 0.3271
     return Ie * torch.exp(-bn * ((R / R_sersic) ** (1 / n_sersic) - 1.0))
+
+
+def core_sersic_light(x, y, R_sersic, n_sersic, Rb, alpha, gamma, e1, e2, center_x, center_y, Ie):
+    """``tf/profiles/light/sersic.py:88-121`` as written, quirks included: the
+    ``- 1.0`` sits inside the exponential but outside the ``-bn * (...)``
+    product, the scaled radius is divided by ``alpha * n`` instead of raised to
+    ``1/(alpha n)``, and ``R_sersic ** alpha ** 1.0`` is ``R_sersic ** alpha``."""
+    R = sersic_distance(x, y, center_x, center_y, e1, e2)
+    bn = 1.9992 * n_sersic - 0.3271
+    return (Ie * (1 + (Rb / R) ** alpha) ** (gamma / alpha)
+            * torch.exp(-bn * ((R ** alpha + Rb ** alpha) / R_sersic ** alpha ** 1.0 / (alpha * n_sersic)) - 1.0))
 
 
 def shapelet_orders(n_max: int) -> Tuple[List[int], List[int]]:
@@ -234,6 +274,8 @@ def _mass(kind, opts, x, y, p, n_terms):
         return sis_deriv(x, y, p["theta_E"], p["center_x"], p["center_y"])
     if kind == "SIE":
         return sie_deriv(x, y, p["theta_E"], p["e1"], p["e2"], p["center_x"], p["center_y"])
+    if kind == "TNFW":
+        return tnfw_deriv(x, y, p["Rs"], p["alpha_Rs"], p["r_trunc"], p["center_x"], p["center_y"])
     raise ValueError(kind)
 
 
@@ -245,6 +287,11 @@ def _light(kind, opts, x, y, p, lstsq=False):
     if kind == "SERSIC":
         Ie = torch.ones_like(p["R_sersic"]) if lstsq else p["Ie"]
         out = sersic_light(x, y, p["R_sersic"], p["n_sersic"], p["center_x"], p["center_y"], Ie)
+        return out[None] if lstsq else out
+    if kind == "CORE_SERSIC":
+        Ie = torch.ones_like(p["R_sersic"]) if lstsq else p["Ie"]
+        out = core_sersic_light(x, y, p["R_sersic"], p["n_sersic"], p["Rb"], p["alpha"], p["gamma"], p["e1"],
+                                p["e2"], p["center_x"], p["center_y"], Ie)
         return out[None] if lstsq else out
     if kind == "SHAPELETS":
         n_max = opts["n_max"]
@@ -421,6 +468,8 @@ PARAM_NAMES = {
     "SIE": ["theta_E", "e1", "e2", "center_x", "center_y"],
     "SERSIC": ["R_sersic", "n_sersic", "center_x", "center_y", "Ie"],
     "SERSIC_ELLIPSE": ["R_sersic", "n_sersic", "e1", "e2", "center_x", "center_y", "Ie"],
+    "TNFW": ["Rs", "alpha_Rs", "r_trunc", "center_x", "center_y"],
+    "CORE_SERSIC": ["R_sersic", "n_sersic", "Rb", "alpha", "gamma", "e1", "e2", "center_x", "center_y", "Ie"],
 }
 
 
@@ -434,7 +483,13 @@ def flat_layout(model, lstsq=False):
     layout = []
     for gi, g in enumerate(groups):
         for pi, (kind, opts) in enumerate(g):
-            names = list(PARAM_NAMES[kind]) if kind != "SHAPELETS" else ["beta", "center_x", "center_y"]
+            if kind == "SHAPELETS":
+                names = ["beta", "center_x", "center_y"]
+                if not (lstsq or opts.get("use_lstsq", False)):
+                    D = (opts["n_max"] + 1) * (opts["n_max"] + 2) // 2
+                    names += [f"amp{str(i).zfill(len(str(D)))}" for i in range(D)]
+            else:
+                names = list(PARAM_NAMES[kind])
             if lstsq and "Ie" in names:
                 names.remove("Ie")
             for k in sorted(names):

@@ -35,7 +35,11 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_abi_version():
-    assert N.lib().gl_abi_version() == 1
+    import re
+
+    with open(os.path.join(HEADER_DIR, "gigalens_cuda.h")) as fh:
+        hv = int(re.search(r"#define GL_ABI_VERSION (\d+)", fh.read()).group(1))
+    assert N.lib().gl_abi_version() == hv == N.GL_ABI_VERSION
 
 
 def test_bad_arguments_are_rejected_without_a_device():

@@ -120,6 +120,9 @@ CONFIGS = {
     "config1_90px_ss2_psf41": (90, 2, 41, 9),
     "ss1_psf13": (48, 1, 13, 5),
     "ss2_nopsf": (40, 2, 0, 4),
+    # PSF sizes k = 3 mod 4 at ss = 2: even sub-kernels, shifted transposed correlation
+    "ss2_psf11": (44, 2, 11, 5),
+    "ss2_psf23": (36, 2, 23, 4),
 }
 
 

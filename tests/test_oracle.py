@@ -134,3 +134,57 @@ def test_oracle_gradient_matches_finite_differences():
         lm, _ = O.forward_log_likelihood_flat(ORACLE_MODEL, cfg, x0 - e, obs, 0.2, 100.0)
         fd = float((lp - lm) / (2 * h))
         assert abs(fd - float(g[0, j])) <= 1e-5 * max(1.0, abs(fd)), (j, fd, float(g[0, j]))
+
+
+def _nfw_alpha(R, Rs, alpha_Rs):
+    """Untruncated NFW deflection with the reference's rho0 convention:
+    |alpha| = 4 rho0 Rs^2 (ln(x/2) + F(x)) / x, which equals alpha_Rs at R = Rs."""
+    rho0 = alpha_Rs / (4.0 * Rs ** 2 * (1.0 + math.log(0.5)))
+    x = R / Rs
+    return 4.0 * rho0 * Rs ** 2 * (torch.log(x / 2) + O.tnfw_F(x)) / x
+
+
+def test_tnfw_untruncated_limit_is_nfw():
+    """tf/profiles/mass/tnfw.py:14-38 reduces to NFW for r_trunc >> Rs; at R = Rs
+    the deflection is alpha_Rs (the parameter's definition)."""
+    Rs, aRs = T(0.7), T(0.3)
+    R = torch.linspace(0.05, 3.0, 301, dtype=D)
+    ax, ay = O.tnfw_deriv(R, torch.zeros_like(R), Rs, aRs, T(1e5), T(0.0), T(0.0))
+    assert torch.allclose(ax, _nfw_alpha(R, Rs, aRs), rtol=1e-5)
+    assert torch.allclose(ay, torch.zeros_like(ay))
+    a1, _ = O.tnfw_deriv(T([0.7]), T([0.0]), Rs, aRs, T(1e5), T(0.0), T(0.0))
+    assert abs(float(a1[0]) - 0.3) < 1e-5
+
+
+def test_tnfw_F_continuous_at_one():
+    x = torch.tensor([1 - 1e-6, 1.0, 1 + 1e-6], dtype=D)
+    F = O.tnfw_F(x)
+    assert torch.allclose(F, torch.ones_like(F), atol=1e-5)
+
+
+def test_tnfw_truncation_reduces_deflection():
+    """Mass beyond r_trunc is removed: at large R the truncated profile deflects less."""
+    R = torch.tensor([5.0, 10.0], dtype=D)
+    full, _ = O.tnfw_deriv(R, torch.zeros_like(R), T(0.7), T(0.3), T(1e5), T(0.0), T(0.0))
+    trunc, _ = O.tnfw_deriv(R, torch.zeros_like(R), T(0.7), T(0.3), T(2.0), T(0.0), T(0.0))
+    assert bool((trunc < full).all())
+
+
+def test_core_sersic_as_written():
+    """tf/profiles/light/sersic.py:88-121 term by term on scalars."""
+    Rs, n, Rb, al, ga, cx, cy, Ie = 0.9, 3.0, 0.1, 2.0, 0.3, 0.05, 0.0, 100.0
+    x, y = 0.4, -0.2
+    R = math.hypot(x - cx, y - cy)          # e1 = e2 = 0
+    bn = 1.9992 * n - 0.3271
+    ref = Ie * (1 + (Rb / R) ** al) ** (ga / al) * math.exp(-bn * ((R ** al + Rb ** al) / Rs ** al / (al * n)) - 1.0)
+    got = O.core_sersic_light(T([x]), T([y]), T(Rs), T(n), T(Rb), T(al), T(ga), T(0.0), T(0.0), T(cx), T(cy), T(Ie))
+    assert abs(float(got[0]) - ref) < 1e-12 * ref
+
+
+def test_flat_layout_explicit_shapelets():
+    """Explicit shapelet amplitudes sort before beta (tf.nest order of the dict keys)."""
+    model = dict(lenses=[("SIS", {})], lens_light=[], source_light=[("SHAPELETS", {"n_max": 3})])
+    names = [k for _, _, k in O.flat_layout(model)]
+    assert names[:3] == ["center_x", "center_y", "theta_E"]
+    assert names[3:13] == ["amp%02d" % i for i in range(10)]
+    assert names[13:] == ["beta", "center_x", "center_y"]
