@@ -415,6 +415,8 @@ static void fill_args(const gl_plan* plan, FusedArgs& a) {
   a.llight = plan->llight;
   a.source = plan->source;
   a.gen = plan->gen;
+  a.gscratch = plan->gscratch;
+  a.cta_floats = plan->cta_floats;
   a.has_prior = plan->has_prior;
   for (int i = 0; i < GL_MAX_PARAMS; ++i) a.prior[i] = plan->prior[i];
   a.img_stride = plan->max_pix;
@@ -524,17 +526,37 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
   plan->smem_bytes = smem_floats * 4;
   const int static_smem = lsq_model ? 0 : fused_static_smem_bytes();
+  (void)static_smem;
   plan->fused_fits = plan->smem_bytes + fused_static_smem_bytes() <= dev_smem;
-  if (!lsq_model && !plan->fused_fits) {
-    set_error("image needs %d bytes of shared memory; the device allows %d per block",
-              plan->smem_bytes + static_smem, dev_smem);
-    delete plan;
-    return GL_ERR_UNSUPPORTED;
-  }
   rc = cuda_check(cudaMalloc((void**)&plan->dev_buf, bytes), "cudaMalloc(plan)");
   if (rc) {
     delete plan;
     return rc;
+  }
+  if (!plan->fused_fits && !lsq_model && plan->family != FAM_GENERIC) {
+    // planes in global memory are a general-path mode
+    rc = resolve_generic(model, false, &plan->gen, &plan->epl, &plan->shear);
+    if (rc) {
+      cudaFree(plan->dev_buf);
+      delete plan;
+      return rc;
+    }
+    plan->family = FAM_GENERIC;
+    plan->gen_ok = 1;
+  }
+  if (!plan->fused_fits && (!lsq_model || plan->gen_ok)) {
+    // the image planes of one CTA exceed shared memory: give every CTA a
+    // slice of global memory (it stays in L2 for the launch)
+    cudaDeviceGetAttribute(&plan->n_cta, cudaDevAttrMultiProcessorCount, plan->device);
+    plan->cta_floats = (int)align_up((size_t)smem_floats, 64);
+    rc = cuda_check(cudaMalloc((void**)&plan->gscratch,
+                               (size_t)plan->n_cta * plan->cta_floats * sizeof(float)),
+                    "cudaMalloc(plane scratch)");
+    if (rc) {
+      cudaFree(plan->dev_buf);
+      delete plan;
+      return rc;
+    }
   }
   plan->dev_buf_bytes = bytes;
   char* base = (char*)plan->dev_buf;
@@ -561,6 +583,7 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
   }
   if (rc) {
     cudaFree(plan->dev_buf);
+    if (plan->gscratch) cudaFree(plan->gscratch);
     delete plan;
     return rc;
   }
@@ -593,6 +616,7 @@ int gl_plan_destroy(gl_plan* plan) {
   if (!plan) return GL_OK;
   lsq_destroy(plan);
   if (plan->dev_buf) cudaFree(plan->dev_buf);
+  if (plan->gscratch) cudaFree(plan->gscratch);
   delete plan;
   return GL_OK;
 }
@@ -767,11 +791,6 @@ int gl_lstsq_grad(const gl_plan* plan, const float* x, const int* img_id, int bs
   }
   if (!plan->gen_ok || plan->gen.n_amp != ((const LsqPlan*)plan->lsq)->D) {
     set_error("gl_lstsq_grad: the model is not supported by the fused kernel's general path");
-    return GL_ERR_UNSUPPORTED;
-  }
-  if (!plan->fused_fits) {
-    set_error("gl_lstsq_grad: the image needs %d bytes of shared memory per CTA, more than the "
-              "device allows", plan->smem_bytes + fused_static_smem_bytes());
     return GL_ERR_UNSUPPORTED;
   }
   int rc = check_device(plan);

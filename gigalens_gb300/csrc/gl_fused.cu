@@ -41,7 +41,8 @@ int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream) {
     cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
     if (g_sm_count <= 0) g_sm_count = 1;
   }
-  const int grid = a.bs < g_sm_count ? a.bs : g_sm_count;
+  int grid = a.bs < g_sm_count ? a.bs : g_sm_count;
+  if (a.gscratch) smem_bytes = 0;   // planes in global memory
   switch (a.family) {
     case FAM_EPL_SHEAR_SE_SE: fam_launch<FAM_EPL_SHEAR_SE_SE>(a, grid, smem_bytes, stream); break;
     case FAM_EPL_SHEAR_SE: fam_launch<FAM_EPL_SHEAR_SE>(a, grid, smem_bytes, stream); break;

@@ -948,7 +948,15 @@ static __device__ void setup_image(const DevImage& I, float* sm) {
 template <int FAM>
 __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constant__ FusedArgs a) {
   extern __shared__ float4 smem_dyn[];
-  float* sm = reinterpret_cast<float*>(smem_dyn);
+  // the image planes: dynamic shared memory, or (general path only) this
+  // CTA's slice of a global, L2-resident scratch when the image does not fit
+  // in shared memory.  The fast families address shared memory directly.
+  float* sm;
+  if constexpr (FAM == FAM_GENERIC)
+    sm = a.gscratch ? a.gscratch + (size_t)blockIdx.x * a.cta_floats
+                    : reinterpret_cast<float*>(smem_dyn);
+  else
+    sm = reinterpret_cast<float*>(smem_dyn);
   __shared__ SmemStatic st;
   const int tid = threadIdx.x;
 

@@ -119,6 +119,8 @@ struct FusedArgs {
   int img_stride;           // floats per sample in img_out
   int zmode;                // 1: x holds z; apply bijector, add prior + fldj
   int want_grad;            // run the adjoint phases
+  float* gscratch;          // images too large for shared memory: per-CTA planes in
+  int cta_floats;           //   global memory (cta_floats per CTA), else null
 };
 
 }  // namespace gl
@@ -140,6 +142,9 @@ struct gl_plan {
   gl::GenArgs gen;          // the model on the fused kernel's general path
   int gen_ok;               // gen describes the model
   int fused_fits;           // the images fit the fused kernel's shared memory
+  float* gscratch;          // otherwise: per-CTA plane storage in global memory
+  int cta_floats;           // floats per CTA in gscratch
+  int n_cta;                // CTAs gscratch holds (the device's SM count)
   void* lsq;                // gl::LsqPlan of the least-squares path, or null
 };
 

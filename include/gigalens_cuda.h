@@ -82,7 +82,11 @@ extern "C" {
  * most 2 mass profiles besides SHEAR (at most one EPL), at most one SHEAR
  * and at most 3 light profiles runs on its general path.  Gradients with
  * respect to explicit shapelet amplitudes are not computed there
- * (GL_ERR_UNSUPPORTED): shapelets take part in gradients with use_lstsq.   */
+ * (GL_ERR_UNSUPPORTED): shapelets take part in gradients with use_lstsq.
+ * Images whose supersampled planes exceed a CTA's shared memory (about 90 x 90
+ * at ss = 2 with a 41-pixel PSF) keep them in a per-CTA slice of a global
+ * scratch owned by the plan: calls on one such plan must not overlap on the
+ * GPU (one stream, or serialised).                                         */
 typedef struct {
   int type;                        /* GL_PROF_*                            */
   int group;                       /* GL_GROUP_*                           */

@@ -123,6 +123,8 @@ CONFIGS = {
     # PSF sizes k = 3 mod 4 at ss = 2: even sub-kernels, shifted transposed correlation
     "ss2_psf11": (44, 2, 11, 5),
     "ss2_psf23": (36, 2, 23, 4),
+    # planes larger than a CTA's shared memory: per-CTA slices of global memory
+    "gmem_100px_ss2_psf21": (100, 2, 21, 3),
 }
 
 

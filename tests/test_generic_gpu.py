@@ -308,11 +308,13 @@ def _oracle_backward(s, x, dtype=torch.float64):
     return O.backward_log_likelihood(im, s["obs"].astype(npd), s["err"].astype(npd))
 
 
-def test_lstsq_grad_matches_oracle_through_pinv():
+@pytest.mark.parametrize("num_pix", [40, 100])
+def test_lstsq_grad_matches_oracle_through_pinv(num_pix):
     """gl_lstsq_grad (envelope theorem at the solved coefficients) against the
     float64 oracle differentiated through pinv, as TensorFlow differentiates
-    tf/model.py:152-158."""
-    s = _lsq_setup()
+    tf/model.py:152-158.  100 px planes exceed shared memory and run from
+    global memory."""
+    s = _lsq_setup(num_pix=num_pix, bs=5 if num_pix < 64 else 3)
     plan = s["sim"].lstsq_plan(s["obs"], s["err"])
     x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
     r = s["sim"].run_lstsq(plan, x, want_image=False, want_loglik=True)
