@@ -32,6 +32,7 @@ import numpy as np
 import torch
 
 from .. import inference as _inf
+from . import distributed as D
 from .model import _LogProb, log_prob_and_grad
 from .optimizers import Adam, AdamState
 from .simulator import LensSimulator
@@ -45,21 +46,27 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
     map_chi2_history = None
 
     def MAP(self, optimizer: Adam = None, start=None, n_samples=500, num_steps=350, seed=0, use_graph=True,
-            stop_chi2=None, check_every=25):
+            stop_chi2=None, check_every=25, distributed=False):
         """Multi-start Adam; returns the unconstrained parameters of all chains.
 
         ``stop_chi2``: stop early once the best chain's chi^2 is <= this value
         (checked every ``check_every`` steps; ``map_steps_run`` records the
-        steps taken)."""
+        steps taken).  ``distributed``: with a process group, this rank runs its
+        contiguous share of the chains (the same chains a single process would
+        run) and returns them; ``best()`` gives the global best chain."""
         optimizer = optimizer if optimizer is not None else Adam(1e-3)
         dev = _cuda_dev()
         prior = self.prob_model.prior
         start = prior.sample(n_samples, seed=seed) if start is None else start
         z0 = torch.as_tensor(self.prob_model.bij.inverse(start), dtype=torch.float32)
+        if distributed:
+            lo, hi = D.shard_range(z0.shape[0])
+            z0 = z0[lo:hi]
         trial = z0.to(dev).contiguous().clone()
         n = trial.shape[0]
         lens_sim = LensSimulator(self.phys_model, self.sim_config, bs=n)
         plan = lens_sim.prob_plan(self.prob_model)
+        self._map_plan = plan
         P = float(self.prob_model.observed_numpy.size)
         logp = torch.empty(n, dtype=torch.float32, device=dev)
         chi2 = torch.empty(n, dtype=torch.float32, device=dev)
@@ -112,12 +119,31 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
         self.map_chi2_history = hist
         self.map_chi2 = chi2
         self.map_log_prob = logp
+        self.map_z = trial
         return trial
 
+    def best(self):
+        """The MAP chain with the highest log posterior (over every rank when
+        the MAP was distributed), as the reference picks the SVI start."""
+        log_prob_and_grad(self._map_plan, self.map_z, self.map_log_prob, self.map_chi2, None)
+        return D.global_best(self.map_z, self.map_log_prob)
+
     # ------------------------------------------------------------------ SVI
-    def SVI(self, optimizer, start, n_vi=250, init_scales=1e-3, num_steps=500, seed=2, use_graph=True):
-        """Returns ``(q_z, losses)`` like the reference (unconstrained space)."""
+    def SVI(self, optimizer, start, n_vi=250, init_scales=1e-3, num_steps=500, seed=2, use_graph=True,
+            distributed=False):
+        """Returns ``(q_z, losses)`` like the reference (unconstrained space).
+
+        ``distributed``: with a process group each rank draws its share of the
+        ``n_vi`` samples (seed + rank) and the ELBO and its gradient are summed
+        over ranks every step (``jax/inference.py:112-117``); steps run eagerly."""
         dev = _cuda_dev()
+        rank, world = D.rank_world() if distributed else (0, 1)
+        n_total = n_vi
+        if world > 1:
+            lo, hi = D.shard_range(n_vi)
+            n_vi = hi - lo
+            seed = seed + rank
+            use_graph = False
         start = torch.as_tensor(start, dtype=torch.float32).reshape(-1).to(dev)
         d = start.numel()
         scale = torch.as_tensor(np.ones(d, np.float32) * init_scales if np.size(init_scales) == 1
@@ -148,9 +174,15 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
             z = theta[:d] + eps @ L.T
             logp, _ = _LogProb.apply(z, plan, None)
             logq = -0.5 * (eps * eps).sum(1) - torch.log(torch.diagonal(L)).sum() - 0.5 * d * log2pi
-            loss = (logq - logp).mean()
+            loss = (logq - logp).sum() / n_total
             (g,) = torch.autograd.grad(loss, theta)
             grad_buf.copy_(g)
+            if world > 1:
+                # the one exchange: ELBO and gradient summed over ranks
+                import torch.distributed as dist
+                dist.all_reduce(grad_buf)
+                loss = loss.detach().clone()
+                dist.all_reduce(loss)
             losses.index_copy_(0, state.step.long().clamp_(max=losses.numel() - 1), loss.detach().reshape(1))
             state.apply(grad_buf)
 
@@ -163,9 +195,16 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
     # ------------------------------------------------------------------ HMC
     def HMC(self, q_z, init_eps=0.3, init_l=3, n_hmc=50, num_burnin_steps=250, num_results=750,
             max_leapfrog_steps=30, seed=3, adapt_trajectory=True, adapt_step_size=True,
-            target_accept_prob=0.75, use_graph=True):
+            target_accept_prob=0.75, use_graph=True, distributed=False):
         """Returns ``(samples, sample_stats)``; samples ``(num_results, n_hmc, d)``
-        in unconstrained space."""
+        in unconstrained space.  ``distributed``: each rank runs its share of
+        the ``n_hmc`` chains (seed + rank) with its own adaptation and returns
+        its samples; ``distributed.gather_chains(samples, dim=1)`` joins them."""
+        if distributed:
+            rank, _ = D.rank_world()
+            lo, hi = D.shard_range(n_hmc)
+            n_hmc = hi - lo
+            seed = seed + rank
         dev = _cuda_dev()
         gen = torch.Generator(device=dev)
         gen.manual_seed(seed)

@@ -96,3 +96,24 @@ def test_map_svi_hmc_sequence_runs(default_prior, default_physmodel):
     rh = potential_scale_reduction(samples.cpu())
     ess = effective_sample_size(samples.cpu())
     assert rh.shape == (22,) and ess.shape == (22,)
+
+
+def test_distributed_flags_single_process(default_prior, default_physmodel):
+    """Without a process group the distributed drivers run every chain, and
+    best() is the argmax of the MAP log posterior."""
+    from gigalens_gb300.cuda.optimizers import Adam
+    from gigalens_gb300.cuda.simulator import LensSimulator
+    from tests.helpers import gaussian_psf
+
+    rng = np.random.default_rng(1)
+    cfg = SimulatorConfig(delta_pix=0.1, num_pix=24, supersample=2, kernel_supersampled=gaussian_psf(0.2, 0.05, 9))
+    truth = default_prior.sample(1, seed=4)
+    img = LensSimulator(default_physmodel, cfg, bs=1).simulate(truth).cpu().numpy()
+    obs = img + rng.normal(scale=0.2, size=img.shape)
+    seq, pm = _seq(default_prior, default_physmodel, data=(obs, 0.2, 100.0), cfg=cfg)
+    z = seq.MAP(Adam(1e-2), n_samples=16, num_steps=10, seed=0, distributed=True)
+    assert z.shape[0] == 16
+    lps, _ = pm.log_prob(LensSimulator(default_physmodel, cfg, bs=16), z)
+    assert torch.equal(seq.best(), z[torch.argmax(lps)])
+    q_z, losses = seq.SVI(Adam(1e-3), seq.best(), n_vi=8, num_steps=3, distributed=True)
+    assert torch.isfinite(losses).all()
