@@ -87,6 +87,11 @@ class gl_model_desc(ctypes.Structure):
     ]
 
 
+class gl_tune_result(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("threads_per_block", "blocks", "samples_per_cta", "smem_bytes",
+                                            "family", "global_planes", "subkernel_side", "col_block")]
+
+
 class gl_image_desc(ctypes.Structure):
     _fields_ = [
         ("num_pix", ctypes.c_int),
@@ -156,6 +161,7 @@ SIGNATURES = [
     ("gl_lstsq", _i, [_vp, _vp, _vp, _i, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp]),
     ("gl_lstsq_noalloc", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
     ("gl_lstsq_grad", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    ("gl_autotune", _i, [_vp, _i, _vp]),
     ("gl_nn_gemm", _i, [_i, _i, _i, _i, _i, _i, ctypes.c_float, _vp, _i, ctypes.c_longlong, _vp, _i,
                         ctypes.c_longlong, ctypes.c_float, _vp, _i, ctypes.c_longlong, _i, _i, _vp]),
     ("gl_nn_im2col3x3", _i, [_vp, _i, _i, _i, _i, _i, _vp, _vp]),

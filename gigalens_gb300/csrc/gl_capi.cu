@@ -779,6 +779,26 @@ int gl_log_prob(const gl_plan* plan, const float* z, const int* img_id, int bs, 
   return launch_fused(a, plan->smem_bytes, (cudaStream_t)stream);
 }
 
+int gl_autotune(const gl_plan* plan, int bs, gl_tune_result* out) {
+  if (!plan || !out || bs < 0) {
+    set_error("gl_autotune: null plan or result, or negative batch");
+    return GL_ERR_INVALID;
+  }
+  int sms = 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
+  memset(out, 0, sizeof(*out));
+  out->threads_per_block = kThreads;
+  out->blocks = bs < sms ? bs : sms;
+  out->samples_per_cta = out->blocks ? (bs + out->blocks - 1) / out->blocks : 0;
+  out->global_planes = plan->gscratch != nullptr;
+  out->smem_bytes = out->global_planes ? 0 : plan->smem_bytes;
+  out->family = plan->family;
+  for (int i = 0; i < plan->n_images; ++i)
+    if (plan->img[i].KS > out->subkernel_side) out->subkernel_side = plan->img[i].KS;
+  out->col_block = kFusedCB;
+  return GL_OK;
+}
+
 int gl_lstsq_grad(const gl_plan* plan, const float* x, const int* img_id, int bs,
                   const float* coeffs, float* logL, float* chi2, float* grad, void* stream) {
   if (!plan || bs < 0 || (bs > 0 && (!x || !coeffs || !grad))) {

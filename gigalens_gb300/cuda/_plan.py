@@ -170,6 +170,12 @@ class Plan:
         if prior is not None:
             self.set_prior(prior)
 
+    def launch_config(self, bs: int) -> dict:
+        """The fused kernel's launch configuration for ``bs`` samples (``gl_autotune``)."""
+        r = N.gl_tune_result()
+        N.call("gl_autotune", self.handle, int(bs), ctypes.byref(r))
+        return {name: getattr(r, name) for name, _ in r._fields_}
+
     def set_prior(self, prior):
         leaves = dist.prior_leaves(prior)
         if len(leaves) != self.d:

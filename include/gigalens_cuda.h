@@ -240,6 +240,24 @@ int gl_lstsq(const gl_plan* plan, const float* x, const int* img_id, int bs, voi
 int gl_lstsq_noalloc(const gl_plan* plan, const float* x, const int* img_id, int bs,
                      float* coeffs, float* img_out, float* logL, float* chi2, void* stream);
 
+/* Launch configuration of the fused kernel for a batch of bs samples.  The
+ * correlation tile (16 outputs per lane, quarter-warp groups of 4 rows x 2
+ * blocks), the block size (512 threads, 16 warps) and the interleave depth
+ * are fixed at compile time for sm_103a; the grid is persistent (one CTA per
+ * SM, at most bs), so there is nothing to search and the result is the
+ * configuration the plan's launches use.                                   */
+typedef struct {
+  int threads_per_block;
+  int blocks;              /* CTAs of a launch of bs samples            */
+  int samples_per_cta;     /* ceil(bs / blocks)                          */
+  int smem_bytes;          /* dynamic shared memory per CTA             */
+  int family;              /* 0..3 compiled fast paths, 4 general path  */
+  int global_planes;       /* 1: the image planes live in global memory */
+  int subkernel_side;      /* largest parity sub-kernel side            */
+  int col_block;           /* correlation outputs per lane              */
+} gl_tune_result;
+int gl_autotune(const gl_plan* plan, int bs, gl_tune_result* out);
+
 /* Gradient of the BackwardProbModel likelihood (tf/model.py:152-158: the
  * least-squares image scored with the data-based error map) with respect to
  * the nonlinear parameters x, at the coefficients gl_lstsq returned for the

@@ -312,3 +312,16 @@ def test_demo_fixture_on_gpu():
     _, ochi2 = O.log_likelihood(im, obs.astype(np.float64), 0.2, 100.0)
     assert abs(float(chi2[0]) - float(ochi2[0])) <= 1e-4 * float(ochi2[0])
     assert 0.97 < float(chi2[0]) < 1.03
+
+
+def test_launch_config_reports_the_kernel_shape():
+    s = _setup(90, 2, gaussian_psf(0.1, 0.0325, 41), 4)
+    plan = s["sim"].prob_plan(s["pm"])
+    c = plan.launch_config(4096)
+    assert c["threads_per_block"] == 512 and c["col_block"] == 16 and c["subkernel_side"] == 21
+    assert c["blocks"] == torch.cuda.get_device_properties(0).multi_processor_count
+    assert c["samples_per_cta"] * c["blocks"] >= 4096 and c["global_planes"] == 0 and c["family"] == 0
+    assert c["smem_bytes"] > 200_000
+    big = _setup(100, 2, gaussian_psf(0.1, 0.0325, 21), 2)
+    cb = big["sim"].prob_plan(big["pm"]).launch_config(3)
+    assert cb["global_planes"] == 1 and cb["smem_bytes"] == 0 and cb["family"] == 4 and cb["blocks"] == 3
