@@ -228,87 +228,12 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
   }
 }
 
-// G_b = X^T W^2 X (upper triangle mirrored), h_b = X^T W^2 y.
-__global__ void __launch_bounds__(256) lsq_gram_kernel(const __grid_constant__ LsqArgs a, float* G,
-                                                       float* h) {
-  __shared__ float xs[kMaxLsqChannels][33];
-  __shared__ float ws[32], ys[32];
-  const int D = a.D;
-  const int ntri = D * (D + 1) / 2;
-  for (int b = blockIdx.x; b < a.bs; b += gridDim.x) {
-    const int im = a.img_id ? a.img_id[b] : 0;
-    if (im < 0 || im >= a.n_images) continue;
-    const LsqImage& I = a.img[im];
-    const int P = I.N * I.N;
-    const float* Xb = a.X + (size_t)b * a.xstride;
-    // entries e = tid + k*256 of the upper triangle (then h): decode (i, j) once
-    constexpr int kMaxE = (kMaxLsqChannels * (kMaxLsqChannels + 1) / 2 + kMaxLsqChannels + 255) / 256;
-    double accv[kMaxE];   // 32-pixel partial sums in float32, accumulated in float64
-    int ei[kMaxE], ej[kMaxE];
-#pragma unroll
-    for (int k = 0; k < kMaxE; ++k) {
-      accv[k] = 0.0;
-      const int e = threadIdx.x + 256 * k;
-      int i = -1, j = -1;
-      if (e < ntri) {
-        int rem = e;
-        i = 0;
-        while (rem >= D - i) {
-          rem -= D - i;
-          ++i;
-        }
-        j = i + rem;
-      } else if (e < ntri + D) {
-        i = e - ntri;
-        j = -2;   // h entry
-      }
-      ei[k] = i;
-      ej[k] = j;
-    }
-    for (int p0 = 0; p0 < P; p0 += 32) {
-      __syncthreads();
-      for (int t = threadIdx.x; t < 32; t += blockDim.x) {
-        const int p = p0 + t;
-        const float w = (p < P) ? 1.f / I.err[p] : 0.f;
-        ws[t] = w;
-        ys[t] = (p < P) ? I.obs[p] * w : 0.f;
-      }
-      __syncthreads();
-      for (int t = threadIdx.x; t < D * 32; t += blockDim.x) {
-        const int c = t >> 5, pp = t & 31;
-        const int p = p0 + pp;
-        xs[c][pp] = (p < P) ? Xb[(size_t)c * I.xcstride + p] * ws[pp] : 0.f;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int k = 0; k < kMaxE; ++k) {
-        const int i = ei[k], j = ej[k];
-        if (i < 0) continue;
-        const float* xj = (j >= 0) ? xs[j] : ys;
-        float s = 0.f;
-#pragma unroll 8
-        for (int pp = 0; pp < 32; ++pp) s = fmaf(xs[i][pp], xj[pp], s);
-        accv[k] += (double)s;
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < kMaxE; ++k) {
-      const int i = ei[k], j = ej[k];
-      if (i < 0) continue;
-      if (j >= 0) {
-        G[((size_t)b * D + i) * D + j] = (float)accv[k];
-        G[((size_t)b * D + j) * D + i] = (float)accv[k];
-      } else {
-        h[(size_t)b * D + i] = (float)accv[k];
-      }
-    }
-  }
-}
-
 // pinv(G) h by cyclic Jacobi (round-robin parallel ordering), one CTA per sample.
 __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const float* __restrict__ G,
                                                         const float* __restrict__ h, float rcond,
-                                                        float* __restrict__ coeffs, int max_sweeps) {
+                                                        float* __restrict__ coeffs, int max_sweeps,
+                                                        float* __restrict__ Vout, float* __restrict__ ilam,
+                                                        const int* __restrict__ status) {
   __shared__ float A[kMaxLsqChannels + 1][kMaxLsqChannels + 1];
   __shared__ float V[kMaxLsqChannels + 1][kMaxLsqChannels + 1];
   __shared__ float cs[kMaxLsqChannels / 2 + 1][2];
@@ -423,47 +348,101 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
       proj[i] = (i < D && fabsf(lam) > cutoff) ? s / lam : 0.f;
     }
     __syncthreads();
-    __shared__ float cvec[kMaxLsqChannels + 1];
-    __shared__ float rvec[kMaxLsqChannels + 1];
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    // the pinv operator, kept for the refinement: V and the kept inverse eigenvalues
+    const bool bad = status && *status;
+    for (int t = threadIdx.x; t < D * D; t += blockDim.x) {
+      const int r = t / D, i = t - r * D;
+      Vout[(size_t)b * D * D + t] = V[r][i];
+    }
+    for (int i = threadIdx.x; i < D; i += blockDim.x) {
+      const float lam = A[i][i];
+      ilam[(size_t)b * D + i] = fabsf(lam) > cutoff ? 1.f / lam : 0.f;
+    }
+    for (int r = threadIdx.x; r < D; r += blockDim.x) {
       float s = 0.f;
       for (int i = 0; i < n; ++i) s = fmaf(V[r][i], proj[i], s);
-      cvec[r] = r < D ? s : 0.f;
+      coeffs[(size_t)b * D + r] = bad ? __int_as_float(0x7fc00000) : s;
     }
-    __syncthreads();
-    // Iterative refinement against the float32 normal equations: the residual
-    // r = h - G c is accumulated in float64 and its pinv image added to c.  It
-    // removes the error of the float32 eigen-solve, to which the likelihood
-    // gradient at the solution is first-order sensitive.
-    const float* Gb = G + (size_t)b * D * D;
-    for (int it = 0; it < 2; ++it) {
-      for (int row = threadIdx.x; row < n; row += blockDim.x) {
-        double acc = row < D ? (double)hs[row] : 0.0;
-        if (row < D)
-          for (int j = 0; j < D; ++j) acc -= (double)Gb[(size_t)row * D + j] * (double)cvec[j];
-        rvec[row] = (float)acc;
-      }
-      __syncthreads();
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        float s = 0.f;
-        for (int r = 0; r < n; ++r) s = fmaf(V[r][i], rvec[r], s);
-        const float lam = A[i][i];
-        proj[i] = (i < D && fabsf(lam) > cutoff) ? s / lam : 0.f;
-      }
-      __syncthreads();
-      for (int r = threadIdx.x; r < D; r += blockDim.x) {
-        float s = 0.f;
-        for (int i = 0; i < n; ++i) s = fmaf(V[r][i], proj[i], s);
-        cvec[r] += s;
-      }
-      __syncthreads();
-    }
-    for (int r = threadIdx.x; r < D; r += blockDim.x) coeffs[(size_t)b * D + r] = cvec[r];
     __syncthreads();
   }
 }
 
 // img = sum_c coeffs_c X_c; BackwardProbModel likelihood with the data error map.
+// Residual of the weighted least-squares problem from the basis itself (not
+// from G): ew_p = W_p^2 (y_p - sum_c X_cp c_c) with the channel sum in float64
+// (c = NULL: ew = W^2 y, whose projection is h = A^T b).
+__global__ void __launch_bounds__(256) lsq_resid_pix_kernel(const __grid_constant__ LsqArgs a,
+                                                            const float* __restrict__ coeffs,
+                                                            float* __restrict__ ew) {
+  const int D = a.D;
+  for (int b = blockIdx.y; b < a.bs; b += gridDim.y) {
+    const int im = a.img_id ? a.img_id[b] : 0;
+    if (im < 0 || im >= a.n_images) continue;
+    const LsqImage& I = a.img[im];
+    const int P = I.N * I.N;
+    const float* Xb = a.X + (size_t)b * a.xstride;
+    const float* cb = coeffs ? coeffs + (size_t)b * D : nullptr;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+      double m = 0.0;
+      if (cb)
+        for (int c = 0; c < D; ++c) m += (double)Xb[(size_t)c * I.xcstride + p] * (double)__ldg(cb + c);
+      const float w = 1.f / I.err[p];
+      ew[(size_t)b * a.maxP + p] = (float)(((double)I.obs[p] - m) * (double)(w * w));
+    }
+  }
+}
+
+// r_c = sum_p X_cp ew_p: one warp per (sample, channel), 32-term float32
+// partial sums combined in float64.
+__global__ void __launch_bounds__(256) lsq_resid_proj_kernel(const __grid_constant__ LsqArgs a,
+                                                             const float* __restrict__ ew,
+                                                             float* __restrict__ r) {
+  const int D = a.D;
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int t = wid; t < a.bs * D; t += nw) {
+    const int b = t / D, c = t - b * D;
+    const int im = a.img_id ? a.img_id[b] : 0;
+    if (im < 0 || im >= a.n_images) continue;
+    const LsqImage& I = a.img[im];
+    const int P = I.N * I.N;
+    const float* x = a.X + (size_t)b * a.xstride + (size_t)c * I.xcstride;
+    const float* e = ew + (size_t)b * a.maxP;
+    double acc = 0.0;
+    for (int p0 = 0; p0 < P; p0 += 32 * 32) {
+      float s = 0.f;
+      for (int p = p0 + lane; p < min(P, p0 + 32 * 32); p += 32) s = fmaf(x[p], e[p], s);
+      acc += (double)s;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) r[(size_t)b * D + c] = (float)acc;
+  }
+}
+
+// Refinement step: c += V diag(ilam) V^T r (the pinv of G applied to the residual).
+__global__ void __launch_bounds__(64) lsq_update_kernel(int bs, int D, const float* __restrict__ V,
+                                                       const float* __restrict__ ilam,
+                                                       const float* __restrict__ r,
+                                                       float* __restrict__ coeffs) {
+  __shared__ float proj[kMaxLsqChannels];
+  for (int b = blockIdx.x; b < bs; b += gridDim.x) {
+    const float* Vb = V + (size_t)b * D * D;
+    for (int i = threadIdx.x; i < D; i += blockDim.x) {
+      float s = 0.f;
+      for (int k = 0; k < D; ++k) s = fmaf(Vb[k * D + i], r[(size_t)b * D + k], s);
+      proj[i] = s * ilam[(size_t)b * D + i];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < D; k += blockDim.x) {
+      float s = 0.f;
+      for (int i = 0; i < D; ++i) s = fmaf(Vb[k * D + i], proj[i], s);
+      coeffs[(size_t)b * D + k] += s;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void __launch_bounds__(256) lsq_image_kernel(const __grid_constant__ LsqArgs a,
                                                         const float* __restrict__ coeffs,
                                                         float* img_out, float* logL, float* chi2) {
@@ -710,11 +689,15 @@ void lsq_destroy(gl_plan* plan) {
   plan->lsq = nullptr;
 }
 
+// Workspace: X [bs][D][maxP], G [bs][D][D], V [bs][D][D], h, r, ilam [bs][D],
+// ew [bs][maxP], status.
 size_t lsq_workspace_bytes(const LsqPlan* L, int bs) {
+  auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   const size_t X = (size_t)bs * L->D * L->maxP * 4;
   const size_t G = (size_t)bs * L->D * L->D * 4;
   const size_t h = (size_t)bs * L->D * 4;
-  return ((X + 255) / 256 + (G + 255) / 256 + (h + 255) / 256) * 256;
+  const size_t ew = (size_t)bs * L->maxP * 4;
+  return up(X) + 2 * up(G) + 3 * up(h) + up(ew) + 256;
 }
 
 int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, float* work,
@@ -744,23 +727,49 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   a.maxP = L->maxP;
   a.max_bands = L->max_bands;
   a.xstride = (size_t)L->D * L->maxP;
+  auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   char* base = (char*)work;
   a.X = (float*)base;
-  base += (((size_t)bs * L->D * L->maxP * 4 + 255) / 256) * 256;
+  base += up((size_t)bs * L->D * L->maxP * 4);
   float* G = (float*)base;
-  base += (((size_t)bs * L->D * L->D * 4 + 255) / 256) * 256;
+  base += up((size_t)bs * L->D * L->D * 4);
+  float* V = (float*)base;
+  base += up((size_t)bs * L->D * L->D * 4);
   float* h = (float*)base;
-  int sms = 1;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
-  const int items = bs * L->max_bands;
-  lsq_basis_kernel<<<items < sms ? items : sms, kThreads, L->smem_bytes, stream>>>(a);
-  lsq_gram_kernel<<<bs < 4 * sms ? bs : 4 * sms, 256, 0, stream>>>(a, G, h);
+  base += up((size_t)bs * L->D * 4);
+  float* r = (float*)base;
+  base += up((size_t)bs * L->D * 4);
+  float* ilam = (float*)base;
+  base += up((size_t)bs * L->D * 4);
+  float* ew = (float*)base;
+  base += up((size_t)bs * L->maxP * 4);
+  int* status = (int*)base;
   float* co = coeffs;
   if (!co) {
     set_error("least squares: coeffs buffer required");
     return GL_ERR_INVALID;
   }
-  lsq_solve_kernel<<<bs < 8 * sms ? bs : 8 * sms, 128, 0, stream>>>(bs, L->D, G, h, 1e-6f, co, 30);
+  int sms = 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
+  const int items = bs * L->max_bands;
+  cudaMemsetAsync(status, 0, sizeof(int), stream);
+  // basis stack, then G = A^T A on the tensor cores (3xTF32)
+  lsq_basis_kernel<<<items < sms ? items : sms, kThreads, L->smem_bytes, stream>>>(a);
+  int rc = launch_gram_tc(a, G, status, bs < 2 * sms ? bs : 2 * sms, stream);
+  if (rc) return rc;
+  // h = A^T b from the basis, c0 = pinv(G) h, then two refinement steps
+  // against the residual of the least-squares problem itself
+  const dim3 pix_grid((L->maxP + 255) / 256 < 8 ? (L->maxP + 255) / 256 : 8, bs < 65535 ? bs : 65535);
+  const int proj_blocks = (bs * L->D + 7) / 8 < 8 * sms ? (bs * L->D + 7) / 8 : 8 * sms;
+  lsq_resid_pix_kernel<<<pix_grid, 256, 0, stream>>>(a, nullptr, ew);
+  lsq_resid_proj_kernel<<<proj_blocks, 256, 0, stream>>>(a, ew, h);
+  lsq_solve_kernel<<<bs < 8 * sms ? bs : 8 * sms, 128, 0, stream>>>(bs, L->D, G, h, 1e-6f, co, 30, V, ilam,
+                                                                  status);
+  for (int it = 0; it < 2; ++it) {
+    lsq_resid_pix_kernel<<<pix_grid, 256, 0, stream>>>(a, co, ew);
+    lsq_resid_proj_kernel<<<proj_blocks, 256, 0, stream>>>(a, ew, r);
+    lsq_update_kernel<<<bs < 8 * sms ? bs : 8 * sms, 64, 0, stream>>>(bs, L->D, V, ilam, r, co);
+  }
   if (img_out || logL || chi2)
     lsq_image_kernel<<<bs < 4 * sms ? bs : 4 * sms, 256, 0, stream>>>(a, co, img_out, logL, chi2);
   cudaError_t e = cudaGetLastError();

@@ -151,3 +151,39 @@ def test_shapelets_light_api(use_lstsq):
     g = got.double().cpu().numpy().reshape(ref.shape)
     assert np.allclose(g, ref.numpy(), rtol=1e-5, atol=1e-4)
     assert np.abs(g - ref.numpy()).max() < 1e-6
+
+
+def test_tensor_core_gram_accuracy():
+    """G = A^T A from the tcgen05 3xTF32 kernel against float64 from the same
+    basis stack (both read from the workspace: X first, then G).  3xTF32
+    keeps about 21 bits per product and the tensor core sums in FP32 within
+    each 1024-pixel segment (segments are summed in FP64): ~5e-6 of max|G|."""
+    import ctypes
+
+    from gigalens_gb300 import _native as N
+    from gigalens_gb300.cuda.simulator import LensSimulator
+
+    n, n_max = 40, 8
+    prior = shapelet_prior(n_max, True)
+    phys, _ = models(n_max, True)
+    ksub = gaussian_psf(0.1, 0.04, 21)
+    cfg = SimulatorConfig(delta_pix=0.08, num_pix=n, supersample=2, kernel_supersampled=ksub)
+    obs = _obs(n, np.random.default_rng(7))
+    err = np.sqrt(0.1 ** 2 + np.clip(obs, 0, None) / 200.0).astype(np.float32)
+    bs = 5
+    sim = LensSimulator(phys, cfg, bs=bs)
+    plan = sim.lstsq_plan(obs, err)
+    x = sim.layout.flatten_params(prior.sample(bs, seed=3))
+    r = sim.run_lstsq(plan, x, want_image=False)
+    torch.cuda.synchronize()
+    D, P = r["D"], n * n
+    up = lambda v: (v + 255) // 256 * 256
+    w8 = r["work"]
+    X = w8[: bs * D * P * 4].view(torch.float32).reshape(bs, D, P).double().cpu()
+    off = up(bs * D * P * 4)
+    G = w8[off: off + bs * D * D * 4].view(torch.float32).reshape(bs, D, D).double().cpu()
+    A = X / torch.as_tensor(err.reshape(-1), dtype=torch.float64)
+    G64 = A @ A.transpose(1, 2)
+    rel = float(((G - G64).abs() / G64.abs().amax(dim=(1, 2), keepdim=True)).max())
+    assert rel < 2e-5, rel
+    assert bool(torch.isfinite(r["coeffs"]).all())
