@@ -215,6 +215,72 @@ def _events(torch, n):
     return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
 
 
+def lstsq_workload(torch, dev, n_big=2048, n_small=512):
+    """The least-squares configuration: EPL + shear lens, shapelet source with
+    n_max = 8 (45 channels) solved linearly, n_big samples of a 100x100 image
+    and n_small of a 60x60 image in one uneven launch.  Returns a callable
+    running gl_lstsq once, the batch size, the workspace size and buffer."""
+    from gigalens_gb300 import _native as N
+    from gigalens_gb300.model import PhysicalModel
+    from gigalens_gb300.simulator import SimulatorConfig
+    from gigalens_gb300 import workloads as W
+    from gigalens_gb300.cuda._plan import ModelLayout, Plan
+    from gigalens_gb300.cuda.profiles.light import shapelets
+    from gigalens_gb300.cuda.profiles.mass import epl, shear
+
+    phys = PhysicalModel([epl.EPL(50), shear.Shear()], [], [shapelets.Shapelets(8, use_lstsq=True, interpolate=False)])
+    lay = ModelLayout(phys)
+    ims = []
+    for n in (100, 60):
+        cfg = SimulatorConfig(delta_pix=W.DELTA_PIX, num_pix=n, supersample=2,
+                              kernel_supersampled=W.gaussian_psf(W.FWHM, W.DELTA_PIX / 2, 21))
+        o = np.random.default_rng(n).normal(scale=0.1, size=(n, n)).astype(np.float32) + 0.5
+        ims.append(dict(sim_config=cfg, observed=o, background_rms=0.1, exp_time=200.0))
+    lplan = Plan(lay, ims)
+    r = np.random.default_rng(3)
+    nb = n_big + n_small
+    cols = {"beta": r.uniform(0.05, 0.2, nb), "center_x": r.normal(0, 0.05, nb), "center_y": r.normal(0, 0.05, nb)}
+    lens = W.draw_params(nb, seed=4)[0]
+    xs = [[lens[0], lens[1]], [{k: torch.tensor(v, dtype=torch.float32) for k, v in cols.items()}]]
+    x = lay.flatten_params(xs)
+    img_id = torch.cat([torch.zeros(n_big, dtype=torch.int32), torch.ones(n_small, dtype=torch.int32)]).to(dev)
+    wb, D = ctypes.c_size_t(0), ctypes.c_int(0)
+    N.call("gl_lstsq_workspace", lplan.handle, nb, ctypes.byref(wb), ctypes.byref(D))
+    work = torch.empty(wb.value, dtype=torch.uint8, device=dev)
+    co = torch.empty(nb, D.value, device=dev)
+    lg = torch.empty(nb, device=dev)
+
+    def lsq():
+        N.call("gl_lstsq", lplan.handle, N.ptr(x), N.ptr(img_id), nb, N.ptr(work), wb.value, N.ptr(co), None,
+               N.ptr(lg), None, N.stream_ptr())
+
+    lsq.plan = lplan
+    return lsq, nb, wb, work
+
+
+def run_lstsq_only(args):
+    """Time the least-squares configuration alone (one gl_lstsq per step)."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lsq, nb, wb, work = lstsq_workload(torch, dev, args.lstsq_big, args.lstsq_small)
+    for _ in range(args.warmup):
+        lsq()
+    torch.cuda.synchronize()
+    ev = _events(torch, 2 * args.steps)
+    for i in range(args.steps):
+        ev[2 * i].record()
+        lsq()
+        ev[2 * i + 1].record()
+    torch.cuda.synchronize()
+    t = sum(ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(args.steps)) / args.steps
+    print(json.dumps({"metric": "lstsq evals/s (%d x 100^2 + %d x 60^2 px, ss=2, shapelets n_max=8, D=45)"
+                                % (args.lstsq_big, args.lstsq_small),
+                      "value": nb / (t * 1e-3), "unit": "evals/s", "ms_per_step": t, "steps": args.steps,
+                      "warmup": args.warmup, "workspace_gb": wb.value / 1e9}), flush=True)
+
+
 def secondary_timings(torch, dev, pm, plan, z):
     """Quick timings of MAP, least squares and HMC at their configurations."""
     from gigalens_gb300 import _native as N
@@ -259,32 +325,7 @@ def secondary_timings(torch, dev, pm, plan, z):
     out["map_350_steps_s_4096x90px"] = out["map_step_ms_4096x90px"] * 350 / 1e3
 
     # least squares, uneven batch: 2048 x 100^2 + 512 x 60^2, shapelets n_max = 8
-    phys = PhysicalModel([epl.EPL(50), shear.Shear()], [], [shapelets.Shapelets(8, use_lstsq=True, interpolate=False)])
-    lay = ModelLayout(phys)
-    ims = []
-    for n in (100, 60):
-        cfg = SimulatorConfig(delta_pix=W.DELTA_PIX, num_pix=n, supersample=2,
-                              kernel_supersampled=W.gaussian_psf(W.FWHM, W.DELTA_PIX / 2, 21))
-        o = np.random.default_rng(n).normal(scale=0.1, size=(n, n)).astype(np.float32) + 0.5
-        ims.append(dict(sim_config=cfg, observed=o, background_rms=0.1, exp_time=200.0))
-    lplan = Plan(lay, ims)
-    r = np.random.default_rng(3)
-    nb = 2560
-    cols = {"beta": r.uniform(0.05, 0.2, nb), "center_x": r.normal(0, 0.05, nb), "center_y": r.normal(0, 0.05, nb)}
-    lens = W.draw_params(nb, seed=4)[0]
-    xs = [[lens[0], lens[1]], [{k: torch.tensor(v, dtype=torch.float32) for k, v in cols.items()}]]
-    x = lay.flatten_params(xs)
-    img_id = torch.cat([torch.zeros(2048, dtype=torch.int32), torch.ones(512, dtype=torch.int32)]).to(dev)
-    wb, D = ctypes.c_size_t(0), ctypes.c_int(0)
-    N.call("gl_lstsq_workspace", lplan.handle, nb, ctypes.byref(wb), ctypes.byref(D))
-    work = torch.empty(wb.value, dtype=torch.uint8, device=dev)
-    co = torch.empty(nb, D.value, device=dev)
-    lg = torch.empty(nb, device=dev)
-
-    def lsq():
-        N.call("gl_lstsq", lplan.handle, N.ptr(x), N.ptr(img_id), nb, N.ptr(work), wb.value, N.ptr(co), None,
-               N.ptr(lg), None, N.stream_ptr())
-
+    lsq, nb, wb, work = lstsq_workload(torch, dev)
     lsq()
     e0, e1 = _events(torch, 2)
     e0.record()
@@ -490,6 +531,10 @@ def main():
                     help="DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one fused launch "
                          "at 4096 chains, from an ncu capture of this workload (recorded in the JSON line)")
     ap.add_argument("--time-to-map", action="store_true")
+    ap.add_argument("--lstsq-only", action="store_true",
+                    help="time only the least-squares configuration (for profiling)")
+    ap.add_argument("--lstsq-big", type=int, default=2048, help="samples of the 100x100 image")
+    ap.add_argument("--lstsq-small", type=int, default=512, help="samples of the 60x60 image")
     ap.add_argument("--ttm-pairs", type=int, default=2_000_000)
     ap.add_argument("--ttm-epochs", type=int, default=20)
     ap.add_argument("--ttm-lenses", type=int, default=256)
@@ -498,6 +543,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.lstsq_only:
+        run_lstsq_only(args)
     else:
         run_ours(args)
 

@@ -37,6 +37,7 @@ constexpr int kSegChunks = 32;             // chunks per TMEM accumulation segme
 constexpr uint32_t kTmemCols = 64;
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr int kGramSmem = 1024 + 2 * kStageBytes + kN * kN * 8;
+constexpr int kRowsPT = kN / (kGT / 32);   // rows of a chunk one thread loads (D <= 64)
 
 __device__ __forceinline__ uint32_t elem_off(int row, int k) {
   return (uint32_t)(row >> 3) * kSBO + (uint32_t)(k >> 2) * kLBO + (uint32_t)(row & 7) * 16u +
@@ -87,6 +88,18 @@ __global__ void __launch_bounds__(kGT) lsq_gram_tc_kernel(const __grid_constant_
     const float* Xb = a.X + (size_t)b * a.xstride;
     const int nchunks = (P + kKC - 1) / kKC;
     int seg_pos = 0;
+    // a thread's values of the next chunk, loaded while the previous MMAs run
+    float pre[kRowsPT];
+    auto load_chunk = [&](int ch) {
+      const int p = ch * kKC + lane;
+      const float w = p < P ? 1.f / I.err[p] : 0.f;
+#pragma unroll
+      for (int k = 0; k < kRowsPT; ++k) {
+        const int r = warp + k * (kGT / 32);
+        pre[k] = (p < P && r < D) ? Xb[(size_t)r * I.xcstride + p] * w : 0.f;
+      }
+    };
+    load_chunk(0);
     for (int ch = 0; ch < nchunks; ++ch, ++gchunk) {
       const int s = gchunk & 1;
       unsigned char* tile_hi = stages + s * kStageBytes;
@@ -100,17 +113,18 @@ __global__ void __launch_bounds__(kGT) lsq_gram_tc_kernel(const __grid_constant_
         }
       }
       // fill: a warp covers one channel row, 32 consecutive pixels (coalesced)
-      const int p0 = ch * kKC;
-      const int p = p0 + lane;
-      const float w = p < P ? 1.f / I.err[p] : 0.f;
-      for (int r = warp; r < D; r += kGT / 32) {
-        const float v = p < P ? Xb[(size_t)r * I.xcstride + p] * w : 0.f;
-        const float hi = to_tf32(v);
-        const float lo = to_tf32(v - hi);
-        const uint32_t off = elem_off(r, lane);
-        *reinterpret_cast<float*>(tile_hi + off) = hi;
-        *reinterpret_cast<float*>(tile_lo + off) = lo;
+#pragma unroll
+      for (int k = 0; k < kRowsPT; ++k) {
+        const int r = warp + k * (kGT / 32);
+        if (r < D) {
+          const float hi = to_tf32(pre[k]);
+          const float lo = to_tf32(pre[k] - hi);
+          const uint32_t off = elem_off(r, lane);
+          *reinterpret_cast<float*>(tile_hi + off) = hi;
+          *reinterpret_cast<float*>(tile_lo + off) = lo;
+        }
       }
+      if (ch + 1 < nchunks) load_chunk(ch + 1);
       fence_proxy_async_smem();
       __syncthreads();
       if (tid == 0) {

@@ -152,72 +152,91 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
       const float g2 = a.has_shear ? lpget(st.x, a.shear.col[1], 0.f) : 0.f;
       const float4* grid = reinterpret_cast<const float4*>(I.grid);
       float2* beta = reinterpret_cast<float2*>(sm + I.offB);
-      const int per_plane = I.brows * I.N;
-      for (int v = tid; v < I.nplanes * per_plane; v += kThreads) {
-        const int pq = v / per_plane;
-        const int r = v - pq * per_plane;
-        const int yr = r / I.N, X = r - yr * I.N;
+      // rows (plane, band row) over warps, columns over lanes
+      for (int row = tid >> 5; row < I.nplanes * I.brows; row += kThreads / 32) {
+        const int pq = row / I.brows, yr = row - pq * I.brows;
         const int Y = Ylo + yr;
-        float2 bt = make_float2(0.f, 0.f);
-        if (Y >= 0 && Y < I.N) {
-          const float4 xy = __ldg(grid + ((size_t)pq * I.N + Y) * I.N + X);
+        float2* brow = beta + (size_t)row * I.N;
+        if (Y < 0 || Y >= I.N) {
+          for (int X = tid & 31; X < I.N; X += 32) brow[X] = make_float2(0.f, 0.f);
+          continue;
+        }
+        const float4* grow = grid + ((size_t)pq * I.N + Y) * I.N;
+        for (int X = tid & 31; X < I.N; X += 32) {
+          const float4 xy = __ldg(grow + X);
           float ax, ay;
           epl_deflect(ec, st.tab, xy.x, xy.y, ax, ay);
-          bt.x = xy.x - ax;
-          bt.y = xy.y - ay;
+          float2 bt = make_float2(xy.x - ax, xy.y - ay);
           if (a.has_shear) {
             bt.x = bt.x - (g1 * xy.x + g2 * xy.y);
             bt.y = bt.y - (g2 * xy.x - g1 * xy.y);
           }
+          brow[X] = bt;
         }
-        beta[v] = bt;
       }
     }
     __syncthreads();
     float* Xb = a.X + (size_t)b * a.xstride;
     for (int c0 = 0; c0 < a.D; c0 += I.CPn) {
-      // evaluate channels c0 .. c0+CPn-1 on the band
-      const int per_plane = I.brows * I.N;
+      // evaluate channels c0 .. c0+CPn-1 on the band: rows (channel slot,
+      // plane, band row) over warps, columns over lanes; per-row constants once
       const float2* beta = reinterpret_cast<const float2*>(sm + I.offB);
       const float4* grid = reinterpret_cast<const float4*>(I.grid);
-      for (int v = tid; v < I.CPn * I.nplanes * per_plane; v += kThreads) {
-        const int slot = v / (I.nplanes * per_plane);
+      const int rows_per_slot = I.nplanes * I.brows;
+      for (int row = tid >> 5; row < I.CPn * rows_per_slot; row += kThreads / 32) {
+        const int slot = row / rows_per_slot;
+        const int rr = row - slot * rows_per_slot;
+        const int pq = rr / I.brows, yr = rr - pq * I.brows;
         const int c = c0 + slot;
-        if (c >= a.D) continue;
-        const int vv = v - slot * I.nplanes * per_plane;
-        const int pq = vv / per_plane;
-        const int r = vv - pq * per_plane;
-        const int yr = r / I.N, X = r - yr * I.N;
         const int Y = Ylo + yr;
-        if (Y < 0 || Y >= I.N) continue;   // stays zero
+        if (c >= a.D || Y < 0 || Y >= I.N) continue;   // rows outside the image stay zero
         const int q = pq - (pq / I.ss) * I.ss;
         const LsqChannel ch = a.ch[c];
         const LsqProfile& pr = a.prof[ch.prof];
-        float px, py;
-        if (pr.group == GL_GROUP_SOURCE) {
-          const float2 bt = beta[vv];
-          px = bt.x;
-          py = bt.y;
-        } else {
-          const float4 xy = __ldg(grid + ((size_t)pq * I.N + Y) * I.N + X);
-          px = xy.x;
-          py = xy.y;
-        }
-        float val;
+        const bool src = pr.group == GL_GROUP_SOURCE;
+        const float2* brow = beta + (size_t)rr * I.N;
+        const float4* grow = grid + ((size_t)pq * I.N + Y) * I.N;
+        float* dst = sm + I.offP + (slot * I.nplanes + pq) * I.brows * I.pitch + yr * I.pitch + I.padI[q];
         if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
-          const float bs_ = lpget(st.x, pr.col[0], 1.f);
-          const float u = (px - lpget(st.x, pr.col[1], 0.f)) / bs_;
-          const float w = (py - lpget(st.x, pr.col[2], 0.f)) / bs_;
-          const float fac = expf(-(u * u + w * w) / 2.f);
-          val = fac * hermite_fn(ch.n1, u, pref) * hermite_fn(ch.n2, w, pref);
+          const float ib = 1.f / lpget(st.x, pr.col[0], 1.f);
+          const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
+          for (int X = tid & 31; X < I.N; X += 32) {
+            float px, py;
+            if (src) {
+              const float2 bt = brow[X];
+              px = bt.x;
+              py = bt.y;
+            } else {
+              const float4 xy = __ldg(grow + X);
+              px = xy.x;
+              py = xy.y;
+            }
+            const float u = (px - cx) * ib, w = (py - cy) * ib;
+            const float fac = expf(-(u * u + w * w) / 2.f);
+            float val = fac * hermite_fn(ch.n1, u, pref) * hermite_fn(ch.n2, w, pref);
+            if (isnan(val)) val = 0.f;
+            dst[X] = val;
+          }
         } else {              // unit-amplitude Sersic
-          const SerC s = sersic_consts(lpget(st.x, pr.col[0], 1.f), lpget(st.x, pr.col[1], 1.f),
-                                       lpget(st.x, pr.col[2], 0.f), lpget(st.x, pr.col[3], 0.f),
-                                       lpget(st.x, pr.col[4], 0.f), lpget(st.x, pr.col[5], 0.f), 1.f);
-          val = sersic_light(s, px, py);
+          const SerC sc = sersic_consts(lpget(st.x, pr.col[0], 1.f), lpget(st.x, pr.col[1], 1.f),
+                                        lpget(st.x, pr.col[2], 0.f), lpget(st.x, pr.col[3], 0.f),
+                                        lpget(st.x, pr.col[4], 0.f), lpget(st.x, pr.col[5], 0.f), 1.f);
+          for (int X = tid & 31; X < I.N; X += 32) {
+            float px, py;
+            if (src) {
+              const float2 bt = brow[X];
+              px = bt.x;
+              py = bt.y;
+            } else {
+              const float4 xy = __ldg(grow + X);
+              px = xy.x;
+              py = xy.y;
+            }
+            float val = sersic_light(sc, px, py);
+            if (isnan(val)) val = 0.f;
+            dst[X] = val;
+          }
         }
-        if (isnan(val)) val = 0.f;
-        sm[I.offP + (slot * I.nplanes + pq) * I.brows * I.pitch + yr * I.pitch + I.padI[q] + X] = val;
       }
       __syncthreads();
 #define GL_CALL_LSQ(KSV) lsq_band_conv<KSV>(I, sm, c0, nb, i0, Xb)
@@ -369,7 +388,8 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
 
 // img = sum_c coeffs_c X_c; BackwardProbModel likelihood with the data error map.
 // Residual of the weighted least-squares problem from the basis itself (not
-// from G): ew_p = W_p^2 (y_p - sum_c X_cp c_c) with the channel sum in float64
+// from G): ew_p = W_p^2 (y_p - sum_c X_cp c_c), the channel sum in float32
+// groups of 8 added in float64
 // (c = NULL: ew = W^2 y, whose projection is h = A^T b).
 __global__ void __launch_bounds__(256) lsq_resid_pix_kernel(const __grid_constant__ LsqArgs a,
                                                             const float* __restrict__ coeffs,
@@ -385,7 +405,11 @@ __global__ void __launch_bounds__(256) lsq_resid_pix_kernel(const __grid_constan
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
       double m = 0.0;
       if (cb)
-        for (int c = 0; c < D; ++c) m += (double)Xb[(size_t)c * I.xcstride + p] * (double)__ldg(cb + c);
+        for (int c0 = 0; c0 < D; c0 += 8) {   // float32 groups of 8 channels, float64 across groups
+          float g = 0.f;
+          for (int c = c0; c < min(D, c0 + 8); ++c) g = fmaf(Xb[(size_t)c * I.xcstride + p], __ldg(cb + c), g);
+          m += (double)g;
+        }
       const float w = 1.f / I.err[p];
       ew[(size_t)b * a.maxP + p] = (float)(((double)I.obs[p] - m) * (double)(w * w));
     }
