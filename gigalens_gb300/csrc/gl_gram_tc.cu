@@ -3,7 +3,7 @@
 // the dense contraction of LensSimulator.lstsq_simulate
 // (gigalens/tf/simulator.py:150-160, X^T W^2 X).
 //
-// One CTA per sample (persistent over the batch), 128 threads.  Pixels are
+// One CTA per sample (persistent over the batch), 256 threads.  Pixels are
 // consumed in chunks of 32: the threads load a chunk of A, split every value
 // into a TF32 head and a TF32 tail (3xTF32: A^T A ~ hi^T hi + hi^T lo + lo^T
 // hi, FP32-level accuracy), and store both into shared memory in the
@@ -26,7 +26,7 @@
 namespace gl {
 
 namespace {
-constexpr int kGT = 128;                   // threads
+constexpr int kGT = 256;                   // threads
 constexpr int kKC = 32;                    // pixels per chunk (K per stage)
 constexpr int kM = 128, kN = 64;           // MMA shape; rows >= D are zero
 constexpr uint32_t kLBO = 144;             // bytes between K-adjacent core matrices
@@ -36,7 +36,8 @@ constexpr int kStageBytes = 2 * kTileBytes;   // hi + lo
 constexpr int kSegChunks = 32;             // chunks per TMEM accumulation segment
 constexpr uint32_t kTmemCols = 64;
 constexpr uint32_t kWaitLimit = 1u << 22;
-constexpr int kGramSmem = 1024 + 2 * kStageBytes + kN * kN * 8;
+constexpr int kG64Ld = kN + 1;              // float64 copy of G: padded rows (bank spread)
+constexpr int kGramSmem = 1024 + 2 * kStageBytes + kN * kG64Ld * 8;
 constexpr int kRowsPT = kN / (kGT / 32);   // rows of a chunk one thread loads (D <= 64)
 
 __device__ __forceinline__ uint32_t elem_off(int row, int k) {
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(kGT) lsq_gram_tc_kernel(const __grid_constant_
   // zero both stages once: rows >= D stay zero for the whole kernel
   for (int i = tid; i < 2 * kStageBytes / 16; i += kGT)
     reinterpret_cast<float4*>(stages)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int i = tid; i < kN * kN; i += kGT) G64[i] = 0.0;
+  for (int i = tid; i < kN * kG64Ld; i += kGT) G64[i] = 0.0;
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
@@ -160,7 +161,7 @@ __global__ void __launch_bounds__(kGT) lsq_gram_tc_kernel(const __grid_constant_
             tc_ld_32x32b_x16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 16), v);
             if (row < D) {
 #pragma unroll
-              for (int i = 0; i < 16; ++i) G64[row * kN + cb * 16 + i] += (double)v[i];
+              for (int i = 0; i < 16; ++i) G64[row * kG64Ld + cb * 16 + i] += (double)v[i];
             }
           }
         }
@@ -173,10 +174,10 @@ __global__ void __launch_bounds__(kGT) lsq_gram_tc_kernel(const __grid_constant_
     // write G (float) and clear the float64 copy for the next sample
     for (int i = tid; i < D * D; i += kGT) {
       const int r = i / D, c = i - r * D;
-      G[(size_t)b * D * D + i] = (float)G64[r * kN + c];
+      G[(size_t)b * D * D + i] = (float)G64[r * kG64Ld + c];
     }
     __syncthreads();
-    for (int i = tid; i < kN * kN; i += kGT) G64[i] = 0.0;
+    for (int i = tid; i < kN * kG64Ld; i += kGT) G64[i] = 0.0;
     __syncthreads();
   }
   if (failed) {
