@@ -105,6 +105,7 @@ static bool resolve_family(const gl_model_desc* m, int* family, DevProfile* epl,
 static int resolve_generic(const gl_model_desc* m, bool lsq, GenArgs* g, DevProfile* epl,
                            DevProfile* shear) {
   memset(g, 0, sizeof(*g));
+  g->amp_grad_slot = -1;
   for (auto* p : {epl, shear}) {
     p->type = GL_PROF_NONE;
     p->niter = 0;
@@ -198,7 +199,7 @@ static int resolve_generic(const gl_model_desc* m, bool lsq, GenArgs* g, DevProf
             return GL_ERR_INVALID;
           }
           L.col[3] = p.col[3];
-          g->explicit_shapelets = 1;
+          if (g->explicit_shapelets++ == 0) g->amp_grad_slot = g->n_light - 1;
         }
       } else {
         set_error("light profile type %d is not a light profile", p.type);
@@ -670,9 +671,9 @@ int gl_plan_query(const gl_plan* plan, int* smem_bytes, int* threads_per_block, 
 }
 
 static int grad_checks(const gl_plan* plan) {
-  if (plan->family == FAM_GENERIC && plan->gen.explicit_shapelets) {
-    set_error("gradients with respect to explicit shapelet amplitudes are not implemented; "
-              "use Shapelets(use_lstsq=True)");
+  if (plan->family == FAM_GENERIC && plan->gen.explicit_shapelets > 1) {
+    set_error("gradients with respect to the amplitudes of more than one explicit shapelet "
+              "profile are not implemented; use Shapelets(use_lstsq=True)");
     return GL_ERR_UNSUPPORTED;
   }
   return GL_OK;

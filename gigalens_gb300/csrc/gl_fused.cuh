@@ -67,6 +67,7 @@ struct SmemStatic {
   // general path
   SerC gser[kGenLight];            // Sersic constants of the light slots
   float amp[kMaxAmps];             // external amplitudes of the current sample
+  float ampg[64];                  // d logL / d (explicit shapelet amplitudes)
   float pref[kMaxShapeletN + 1];   // shapelet normalisations 1/sqrt(2^n sqrt(pi) n!)
 };
 
@@ -768,6 +769,53 @@ static __device__ void phase_pixels_forward_gen(const FusedArgs& a, const DevIma
   }
 }
 
+// (n1, n2) of shapelet basis function k in the reference's order
+// (0,0), (1,0), (0,1), (2,0), (1,1), (0,2), ...
+__host__ __device__ constexpr int shp_order(int k) {
+  int m = 0;
+  while ((m + 1) * (m + 2) / 2 <= k) ++m;
+  return m;
+}
+__host__ __device__ constexpr int shp_n2(int k) { return k - shp_order(k) * (shp_order(k) + 1) / 2; }
+__host__ __device__ constexpr int shp_n1(int k) { return shp_order(k) - shp_n2(k); }
+
+// Adds one pixel's amplitude-gradient contributions g * basis_k(u, v) of an
+// explicit shapelet profile to the warp's running sums: a reduce-scatter over
+// the warp leaves lane l with the sums of amplitudes l and 32 + l.  Every
+// lane of the warp calls it (g = 0 where a lane has no pixel).
+static __device__ __forceinline__ void shapelet_amp_grad(float g, float u, float v, int nmax,
+                                                         const float* pref, float& acc_lo,
+                                                         float& acc_hi) {
+  const int lane = threadIdx.x & 31;
+  float pu[kMaxShapeletN + 1], pv[kMaxShapeletN + 1];
+  shapelet_phis(u, nmax, pref, pu);
+  shapelet_phis(v, nmax, pref, pv);
+  const float fg = g * expf(-(u * u + v * v) / 2.f);
+  const int D = (nmax + 1) * (nmax + 2) / 2;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float w[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int k = 32 * h + j;
+      constexpr int kMaxD = (kMaxShapeletN + 1) * (kMaxShapeletN + 2) / 2;
+      w[j] = (k < kMaxD && k < D) ? fg * pu[k < kMaxD ? shp_n1(k) : 0] * pv[k < kMaxD ? shp_n2(k) : 0] : 0.f;
+    }
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+      const bool up = (lane & off) != 0;
+#pragma unroll
+      for (int j = 0; j < off; ++j) {
+        const float send = up ? w[j] : w[j + off];
+        const float keep = up ? w[j + off] : w[j];
+        w[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+      }
+    }
+    if (h == 0) acc_lo += w[0];
+    else acc_hi += w[0];
+  }
+}
+
 // Phase 4 (general path).
 static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevImage& I, const float* sm,
                                          SmemStatic& st, int K) {
@@ -782,7 +830,14 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
   ea.zero();
   const int total = I.nplanes * I.N * I.N;
   const float4* grid = reinterpret_cast<const float4*>(I.grid);
-  for (int px = threadIdx.x; px < total; px += kThreads) {
+  const int lane = threadIdx.x & 31;
+  const int as = g.amp_grad_slot;   // explicit shapelet slot, or -1
+  float amp_lo = 0.f, amp_hi = 0.f;
+  // the warp's lanes iterate together (the amplitude gradients reduce over the warp)
+  for (int base = threadIdx.x - lane; base < total; base += kThreads) {
+    const int px = base + lane;
+    float ga = 0.f, su = 0.f, sv = 0.f;   // amplitude-gradient inputs of this pixel
+    if (px < total) {
     const float4 xy = __ldg(grid + px);
     const float gimg = sm[__float_as_int(xy.z)];
     // deflection (the EPL keeps its series state for the reverse)
@@ -815,7 +870,15 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
         const bool src = g.light[l].group == GL_GROUP_SOURCE;
         img += gen_light(g.light[l], l, st, src ? bx : xy.x, src ? by : xy.y);
       }
-    if (isnan(img)) continue;   // the reference zeroes NaN pixels: no gradient flows
+    if (!isnan(img)) {   // the reference zeroes NaN pixels: no gradient flows
+    if (as >= 0) {
+      const GenLight& L = g.light[as];
+      const bool src = L.group == GL_GROUP_SOURCE;
+      const float beta = pget(st.x, L.col[0], 1.f);
+      su = ((src ? bx : xy.x) - pget(st.x, L.col[1], 0.f)) / beta;
+      sv = ((src ? by : xy.y) - pget(st.x, L.col[2], 0.f)) / beta;
+      ga = gimg;
+    }
     // light reverse; the sources give the adjoint of beta
     float bxb = 0.f, byb = 0.f;
 #pragma unroll
@@ -843,6 +906,9 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
         else
           gen_mass_reverse(g.mass[s], st.x, xy.x, xy.y, abx, aby, acc + G_MASS + 8 * s);
       }
+    }   // !isnan(img)
+    }   // px < total
+    if (as >= 0) shapelet_amp_grad(ga, su, sv, g.light[as].n_max, st.pref, amp_lo, amp_hi);
   }
   // the EPL slot's accumulators
 #pragma unroll
@@ -852,7 +918,22 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
       e[0] = ea.phi; e[1] = ea.SP; e[2] = ea.SPlnR; e[3] = ea.FH;
       e[4] = ea.FT; e[5] = ea.q; e[6] = ea.cx; e[7] = ea.cy;
     }
-  block_reduce<G_NACC>(acc, st);
+  block_reduce<G_NACC>(acc, st);   // ends with a barrier: st.red is free again
+  if (as >= 0) {
+    // amplitude gradients: the warps' lane sums, over the warps
+    const int warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      st.red[warp][lane] = h == 0 ? amp_lo : amp_hi;
+      __syncthreads();
+      if (threadIdx.x < 32) {
+        float s = 0.f;
+        for (int w = 0; w < kWarps; ++w) s += st.red[w][threadIdx.x];
+        st.ampg[32 * h + threadIdx.x] = s;
+      }
+      __syncthreads();
+    }
+  }
 }
 
 // Per-sample chain rule of the general path (thread 0).
@@ -900,6 +981,10 @@ static __device__ void sample_chain_gen(const FusedArgs& a, SmemStatic& st, int 
       scatter(st.gx, cols, e, 10);
     } else if (L.type == GL_PROF_SHAPELETS) {
       scatter(st.gx, L.col, e, 3);
+      if (l == g.amp_grad_slot) {
+        const int D = (L.n_max + 1) * (L.n_max + 2) / 2;
+        for (int k = 0; k < D; ++k) st.gx[L.col[3] + k] += st.ampg[k];
+      }
     }
   }
 }

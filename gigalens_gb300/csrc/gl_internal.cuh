@@ -93,7 +93,8 @@ struct GenArgs {
   const float* amps;           // [bs, n_amp] or null
   int noise_err;               // data-noise likelihood with the image's error map
   int unit_cf;                 // images without the conversion factor (least-squares images)
-  int explicit_shapelets;      // a shapelet profile with amplitude parameters (no gradient)
+  int explicit_shapelets;      // shapelet profiles with amplitude parameters
+  int amp_grad_slot;           // the light slot whose amplitude gradients are reduced, or -1
 };
 
 struct FusedArgs {

@@ -81,8 +81,8 @@ extern "C" {
  * SERSIC / SERSIC_ELLIPSE lens light and source; every other model with at
  * most 2 mass profiles besides SHEAR (at most one EPL), at most one SHEAR
  * and at most 3 light profiles runs on its general path.  Gradients with
- * respect to explicit shapelet amplitudes are not computed there
- * (GL_ERR_UNSUPPORTED): shapelets take part in gradients with use_lstsq.
+ * respect to explicit shapelet amplitudes are computed for one shapelet
+ * profile per model (more give GL_ERR_UNSUPPORTED).
  * Images whose supersampled planes exceed a CTA's shared memory (about 90 x 90
  * at ss = 2 with a 41-pixel PSF) keep them in a per-CTA slice of a global
  * scratch owned by the plan: calls on one such plan must not overlap on the

@@ -126,10 +126,10 @@ def _setup(name, num_pix=40, ss=2, k=13, bs=6, seed=0):
                 x_struct=prior.sample(bs, seed=seed))
 
 
-GRAD_CASES = ["sie_shear_coresersic_se", "epl_tnfw_shear_se", "sis_se_two_sources"]
+GRAD_CASES = ["sie_shear_coresersic_se", "epl_tnfw_shear_se", "sis_se_two_sources", "sis_shapelets_explicit"]
 
 
-@pytest.mark.parametrize("name", GRAD_CASES + ["sis_shapelets_explicit"])
+@pytest.mark.parametrize("name", GRAD_CASES)
 def test_general_path_simulate(name):
     s = _setup(name)
     img = s["sim"].simulate(s["x_struct"])
@@ -185,23 +185,19 @@ def test_general_path_log_prob_autograd():
     _check_grad(z.grad, (gz, band), "dlogp/dz")
 
 
-def test_explicit_shapelet_gradient_is_refused():
-    s = _setup("sis_shapelets_explicit", bs=3)
-    plan = s["sim"].prob_plan(s["pm"])
-    x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
-    grad = torch.empty_like(x)
-    rc = N.lib().gl_forward_grad(plan.handle, N.ptr(x), None, 3, None, None, N.ptr(grad), None, N.stream_ptr())
-    assert rc == N.GL_ERR_UNSUPPORTED
-    assert b"shapelet" in N.lib().gl_last_error()
-    # the value path works
-    logL = torch.empty(3, device="cuda")
-    chi2 = torch.empty(3, device="cuda")
-    N.call("gl_forward", plan.handle, N.ptr(x), None, 3, N.ptr(logL), N.ptr(chi2), None, None, N.stream_ptr())
-    torch.cuda.synchronize()
-    ll, c2 = O.forward_log_likelihood_flat(s["om"], s["ocfg"], x.double().cpu(), s["obs"].astype(np.float64), 0.2,
-                                           1000.0)
-    _check_scalar(logL, ll, 1e-4, name="logL")
-    _check_scalar(chi2, c2, 1e-4, name="chi2")
+def test_explicit_shapelet_amplitude_gradients_drive_map():
+    """With explicit shapelet amplitudes (Shapelets(use_lstsq=False)) the MAP
+    runs on the general path and raises the log posterior."""
+    from gigalens_gb300.cuda.inference import ModellingSequence
+    from gigalens_gb300.cuda.optimizers import Adam
+
+    s = _setup("sis_shapelets_explicit", bs=8, seed=4)
+    seq = ModellingSequence(s["phys"], s["pm"], s["sim"].sim_config)
+    z0 = s["pm"].bij.inverse(s["x_struct"]).float()
+    lp0, _ = s["pm"].log_prob(s["sim"], z0.cuda())
+    z = seq.MAP(Adam(1e-2), start=s["x_struct"], num_steps=60)
+    lp1, _ = s["pm"].log_prob(s["sim"], z)
+    assert torch.isfinite(lp1).all() and float(lp1.max()) > float(lp0.max())
 
 
 def _value_band(fn, args64, n_perturb=8, seed=0):
