@@ -1,12 +1,15 @@
 // Linear-amplitude path: LensSimulator.lstsq_simulate (tf/simulator.py:99-165).
 //
-//   basis kernel   per (sample, band of output rows): ray-trace the band's
-//                  supersampled pixels once (beta kept in shared memory), then
-//                  for every basis channel (unit-amplitude lens-light Sersic,
+//   basis kernel   per (sample, band of output rows; the whole image when
+//                  one channel's parity planes fit in shared memory):
+//                  ray-trace the band's supersampled pixels once into the
+//                  CTA's slice of a global scratch (L2-resident), then for
+//                  every basis channel (unit-amplitude lens-light Sersic,
 //                  shapelet (n1, n2) functions of the source) evaluate the
-//                  channel on the band, apply PSF + binning with the same
-//                  parity-plane correlation as the fused kernel, and store the
-//                  binned basis X[b][c][pixel] (unweighted, as `ret`)
+//                  channel into the parity planes, apply PSF + binning with
+//                  the register-blocked row correlation of the fused kernel,
+//                  and store the binned basis X[b][c][pixel] (unweighted, as
+//                  `ret`)
 //   gram kernel    G_b = X^T W^2 X and h_b = X^T W^2 y, W = 1/err_map
 //   solve kernel   coeffs = pinv(G, rcond=1e-6) h: cyclic Jacobi
 //                  eigen-decomposition of the symmetric G (for a symmetric
@@ -16,6 +19,7 @@
 //   image kernel   img = sum_c coeffs_c X_c (no conversion factor, as the
 //                  reference), Gaussian log-likelihood with the data-based
 //                  error map and chi^2 (BackwardProbModel, tf/model.py:157-163)
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -82,34 +86,59 @@ __device__ void lsq_term_counts(const LsqArgs& a, LsqShared& st) {
   }
 }
 
-// Correlation of one band: output rows [i0, i0+nb) of channel slot cc.
-template <int KS>
-__device__ void lsq_band_conv(const LsqImage& I, const float* sm, int cc, int nb, int i0,
-                              float* __restrict__ Xout /* X[b][c] base */) {
-  const int units = nb * I.ncb;
-  for (int u = threadIdx.x; u < units * I.CPn; u += kThreads) {
-    const int slot = u / units;
-    if (slot + cc >= I.cpass) continue;
-    const int uu = u - slot * units;
-    const int il = uu / I.ncb, cb = uu - il * I.ncb;
-    const int j0 = kColBlock * cb;
-    if (j0 >= I.N) continue;
-    float acc[kColBlock];
+// i / div for 0 <= i < 2^21 through the float reciprocal inv = 1/div: the
+// quotient (i + 0.5) / div lies at least 0.5 / div from an integer, and the
+// product's relative error (three roundings, < 2e-7) moves it by less than
+// (i + 0.5) * 2e-7 / div < 0.5 / div.  The host checks the index bound.
+__device__ __forceinline__ int small_div(int i, float inv) {
+  return __float2int_rz(((float)i + 0.5f) * inv);
+}
+
+// PSF + binning of one pass: output rows [i0, i0 + nb) of the channels
+// c0 .. c0 + CPn - 1 held in the planes.  A unit is (channel slot, column
+// block, output row) with the row fastest, so the eight threads of a
+// 16-byte load phase read eight consecutive plane rows of one column block:
+// with pitch / 4 odd they fall into eight distinct bank groups.
+template <int KS, int CB>
+__device__ void lsq_pass_conv(const LsqImage& I, const float* sm, int c0, int nb, int i0,
+                              float* __restrict__ Xout /* X[b][0] */) {
+  const int units = I.CPn * I.ncbC * nb;
+  const float* kern = sm + I.offK;
+  for (int u = threadIdx.x; u < units; u += kThreads) {
+    const int rest = u / nb;
+    const int il = u - rest * nb;
+    const int slot = rest / I.ncbC;
+    const int cb = rest - slot * I.ncbC;
+    if (c0 + slot >= I.cpass) continue;
+    const int j0 = cb * CB;
+    float acc[CB];
 #pragma unroll
-    for (int c = 0; c < kColBlock; ++c) acc[c] = 0.f;
+    for (int c = 0; c < CB; ++c) acc[c] = 0.f;
+    const float* sbase = sm + (size_t)slot * I.nplanes * I.plane_floats + j0;
     for (int pq = 0; pq < I.nplanes; ++pq) {
-      const int q = pq - (pq / I.ss) * I.ss;
-      const float* plane = sm + I.offP + (slot * I.nplanes + pq) * I.brows * I.pitch + I.padI[q] - I.d[q] + j0;
-      const float* kp = sm + I.offK + pq * KS * I.ksp;
-#pragma unroll 1
-      for (int m = 0; m < KS; ++m) corr_row<KS, false>(plane + (il + m) * I.pitch, kp + m * I.ksp, acc);
+      const int p = pq / I.ss;
+      // output row i0 + il of parity p reads plane rows i0 + il - d[p] + m
+      const float* seg = sbase + pq * I.plane_floats + (il + I.R0 - I.d[p]) * I.pitch;
+      corr_rows<KS, false, CB>(seg, I.pitch, kern + pq * KS * I.ksp, I.ksp, KS, acc);
     }
-    float* dst = Xout + (size_t)(cc + slot) * I.xcstride + (size_t)(i0 + il) * I.N + j0;
+    float* dst = Xout + (size_t)(c0 + slot) * I.xcstride + (size_t)(i0 + il) * I.N + j0;
 #pragma unroll
-    for (int c = 0; c < kColBlock; ++c)
+    for (int c = 0; c < CB; ++c)
       if (j0 + c < I.N) dst[c] = acc[c];
   }
 }
+
+// Column blocks of 20 for sub-kernels up to 15 taps (register budget), 16 otherwise.
+#define GL_LSQ_CONV(KSV)                                                     \
+  do {                                                                       \
+    if constexpr (KSV <= 15) {                                               \
+      if (I.CB == 20) {                                                      \
+        lsq_pass_conv<KSV, 20>(I, sm, c0, nb, i0, Xb);                       \
+        break;                                                               \
+      }                                                                      \
+    }                                                                        \
+    lsq_pass_conv<KSV, 16>(I, sm, c0, nb, i0, Xb);                           \
+  } while (0)
 
 __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_constant__ LsqArgs a) {
   extern __shared__ float4 smem_dyn[];
@@ -123,6 +152,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
     pref[tid] = (float)(1.0 / sqrt(pow(2.0, tid) * sqrt(3.14159265358979323846) * f));
   }
   lsq_term_counts(a, st);
+  float2* beta = a.beta + (size_t)blockIdx.x * a.beta_stride;
   const int total = a.bs * a.max_bands;
   for (int item = blockIdx.x; item < total; item += gridDim.x) {
     const int b = item / a.max_bands, band = item - b * a.max_bands;
@@ -132,10 +162,14 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
     if (band >= I.nbands) continue;
     const int i0 = band * I.Bo;
     const int nb = min(I.Bo, I.N - i0);
-    const int Ylo = i0 - I.d[0];            // plane row of band row 0
+    const int Ybase = i0 - I.R0;                        // plane row of shared-memory row 0
+    const int Ya = max(0, Ybase), Yb = min(I.N, Ybase + I.brows);
+    const int nrows = Yb - Ya;                          // plane rows inside the image
+    const int per_plane = nrows * I.N;
+    const float inv_n = 1.f / (float)I.N;
     if (tid < a.d) st.x[tid] = a.x[(size_t)b * a.d + tid];
-    // zero planes (rows outside the image stay zero), load sub-kernels
-    for (int i = tid; i < I.offK; i += kThreads) sm[i] = 0.f;
+    // zero the planes (halo rows and columns stay zero), load the sub-kernels
+    for (int i = tid; i < I.offK / 4; i += kThreads) smem_dyn[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int i = tid; i < I.nplanes * I.KS * I.ksp; i += kThreads) sm[I.offK + i] = __ldg(I.kern + i);
     __syncthreads();
     const int K = st.K[im];
@@ -144,26 +178,18 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
       epl_build_table(st.tab, epl_f_of(lpget(st.x, e[2], 0.f), lpget(st.x, e[3], 0.f)),
                       lpget(st.x, e[1], 2.f) - 1.f, K, tid);
     __syncthreads();
-    // ray-trace the band: beta per (plane, band row, column)
+    const float4* grid = reinterpret_cast<const float4*>(I.grid);
+    // ray-trace the band's supersampled pixels once: beta[(pq, row, X)]
     {
       const EplC ec = epl_consts(lpget(st.x, e[0], 0.f), lpget(st.x, e[1], 2.f), lpget(st.x, e[2], 0.f),
                                  lpget(st.x, e[3], 0.f), lpget(st.x, e[4], 0.f), lpget(st.x, e[5], 0.f), K);
       const float g1 = a.has_shear ? lpget(st.x, a.shear.col[0], 0.f) : 0.f;
       const float g2 = a.has_shear ? lpget(st.x, a.shear.col[1], 0.f) : 0.f;
-      const float4* grid = reinterpret_cast<const float4*>(I.grid);
-      float2* beta = reinterpret_cast<float2*>(sm + I.offB);
-      // rows (plane, band row) over warps, columns over lanes
-      for (int row = tid >> 5; row < I.nplanes * I.brows; row += kThreads / 32) {
-        const int pq = row / I.brows, yr = row - pq * I.brows;
-        const int Y = Ylo + yr;
-        float2* brow = beta + (size_t)row * I.N;
-        if (Y < 0 || Y >= I.N) {
-          for (int X = tid & 31; X < I.N; X += 32) brow[X] = make_float2(0.f, 0.f);
-          continue;
-        }
-        const float4* grow = grid + ((size_t)pq * I.N + Y) * I.N;
-        for (int X = tid & 31; X < I.N; X += 32) {
-          const float4 xy = __ldg(grow + X);
+      for (int pq = 0; pq < I.nplanes; ++pq) {
+        const float4* gp = grid + ((size_t)pq * I.N + Ya) * I.N;
+        float2* bp = beta + (size_t)pq * per_plane;
+        for (int i = tid; i < per_plane; i += kThreads) {
+          const float4 xy = __ldg(gp + i);
           float ax, ay;
           epl_deflect(ec, st.tab, xy.x, xy.y, ax, ay);
           float2 bt = make_float2(xy.x - ax, xy.y - ay);
@@ -171,81 +197,75 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
             bt.x = bt.x - (g1 * xy.x + g2 * xy.y);
             bt.y = bt.y - (g2 * xy.x - g1 * xy.y);
           }
-          brow[X] = bt;
+          bp[i] = bt;
         }
       }
     }
     __syncthreads();
     float* Xb = a.X + (size_t)b * a.xstride;
     for (int c0 = 0; c0 < a.D; c0 += I.CPn) {
-      // evaluate channels c0 .. c0+CPn-1 on the band: rows (channel slot,
-      // plane, band row) over warps, columns over lanes; per-row constants once
-      const float2* beta = reinterpret_cast<const float2*>(sm + I.offB);
-      const float4* grid = reinterpret_cast<const float4*>(I.grid);
-      const int rows_per_slot = I.nplanes * I.brows;
-      for (int row = tid >> 5; row < I.CPn * rows_per_slot; row += kThreads / 32) {
-        const int slot = row / rows_per_slot;
-        const int rr = row - slot * rows_per_slot;
-        const int pq = rr / I.brows, yr = rr - pq * I.brows;
-        const int c = c0 + slot;
-        const int Y = Ylo + yr;
-        if (c >= a.D || Y < 0 || Y >= I.N) continue;   // rows outside the image stay zero
-        const int q = pq - (pq / I.ss) * I.ss;
-        const LsqChannel ch = a.ch[c];
+      // evaluate channels c0 .. c0+CPn-1 on the band's rows inside the image
+      for (int slot = 0; slot < I.CPn && c0 + slot < a.D; ++slot) {
+        const LsqChannel ch = a.ch[c0 + slot];
         const LsqProfile& pr = a.prof[ch.prof];
         const bool src = pr.group == GL_GROUP_SOURCE;
-        const float2* brow = beta + (size_t)rr * I.N;
-        const float4* grow = grid + ((size_t)pq * I.N + Y) * I.N;
-        float* dst = sm + I.offP + (slot * I.nplanes + pq) * I.brows * I.pitch + yr * I.pitch + I.padI[q];
-        if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
-          const float ib = 1.f / lpget(st.x, pr.col[0], 1.f);
-          const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
-          for (int X = tid & 31; X < I.N; X += 32) {
-            float px, py;
-            if (src) {
-              const float2 bt = brow[X];
-              px = bt.x;
-              py = bt.y;
-            } else {
-              const float4 xy = __ldg(grow + X);
-              px = xy.x;
-              py = xy.y;
+        float* sbase = sm + (size_t)slot * I.nplanes * I.plane_floats + (Ya - Ybase) * I.pitch;
+        for (int pq = 0; pq < I.nplanes; ++pq) {
+          const int q = pq - (pq / I.ss) * I.ss;
+          float* pbase = sbase + pq * I.plane_floats + I.padI[q];
+          const float2* bp = beta + (size_t)pq * per_plane;
+          const float4* gp = grid + ((size_t)pq * I.N + Ya) * I.N;
+          if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
+            const float ib = 1.f / lpget(st.x, pr.col[0], 1.f);
+            const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
+            for (int i = tid; i < per_plane; i += kThreads) {
+              float px, py;
+              if (src) {
+                const float2 bt = bp[i];
+                px = bt.x;
+                py = bt.y;
+              } else {
+                const float4 xy = __ldg(gp + i);
+                px = xy.x;
+                py = xy.y;
+              }
+              const float u = (px - cx) * ib, w = (py - cy) * ib;
+              const float fac = expf(-(u * u + w * w) / 2.f);
+              float val = fac * hermite_fn(ch.n1, u, pref) * hermite_fn(ch.n2, w, pref);
+              if (isnan(val)) val = 0.f;
+              const int r = small_div(i, inv_n);
+              pbase[r * I.pitch + (i - r * I.N)] = val;
             }
-            const float u = (px - cx) * ib, w = (py - cy) * ib;
-            const float fac = expf(-(u * u + w * w) / 2.f);
-            float val = fac * hermite_fn(ch.n1, u, pref) * hermite_fn(ch.n2, w, pref);
-            if (isnan(val)) val = 0.f;
-            dst[X] = val;
-          }
-        } else {              // unit-amplitude Sersic
-          const SerC sc = sersic_consts(lpget(st.x, pr.col[0], 1.f), lpget(st.x, pr.col[1], 1.f),
-                                        lpget(st.x, pr.col[2], 0.f), lpget(st.x, pr.col[3], 0.f),
-                                        lpget(st.x, pr.col[4], 0.f), lpget(st.x, pr.col[5], 0.f), 1.f);
-          for (int X = tid & 31; X < I.N; X += 32) {
-            float px, py;
-            if (src) {
-              const float2 bt = brow[X];
-              px = bt.x;
-              py = bt.y;
-            } else {
-              const float4 xy = __ldg(grow + X);
-              px = xy.x;
-              py = xy.y;
+          } else {              // unit-amplitude Sersic
+            const SerC sc = sersic_consts(lpget(st.x, pr.col[0], 1.f), lpget(st.x, pr.col[1], 1.f),
+                                          lpget(st.x, pr.col[2], 0.f), lpget(st.x, pr.col[3], 0.f),
+                                          lpget(st.x, pr.col[4], 0.f), lpget(st.x, pr.col[5], 0.f), 1.f);
+            for (int i = tid; i < per_plane; i += kThreads) {
+              float px, py;
+              if (src) {
+                const float2 bt = bp[i];
+                px = bt.x;
+                py = bt.y;
+              } else {
+                const float4 xy = __ldg(gp + i);
+                px = xy.x;
+                py = xy.y;
+              }
+              float val = sersic_light(sc, px, py);
+              if (isnan(val)) val = 0.f;
+              const int r = small_div(i, inv_n);
+              pbase[r * I.pitch + (i - r * I.N)] = val;
             }
-            float val = sersic_light(sc, px, py);
-            if (isnan(val)) val = 0.f;
-            dst[X] = val;
           }
         }
       }
       __syncthreads();
-#define GL_CALL_LSQ(KSV) lsq_band_conv<KSV>(I, sm, c0, nb, i0, Xb)
-      GL_KS_DISPATCH(I.KS, GL_CALL_LSQ)
-#undef GL_CALL_LSQ
+      GL_KS_DISPATCH(I.KS, GL_LSQ_CONV)
       __syncthreads();
     }
   }
 }
+#undef GL_LSQ_CONV
 
 // pinv(G) h by cyclic Jacobi (round-robin parallel ordering), one CTA per sample.
 __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const float* __restrict__ G,
@@ -603,6 +623,7 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
   const int static_bytes = 8 * 1024;
   int maxP = 0, smem = 0, max_bands = 0;
+  size_t beta_per_cta = 0;
   for (int i = 0; i < plan->n_images; ++i) {
     const DevImage& F = plan->img[i];
     LsqImage& I = L->img[i];
@@ -615,61 +636,74 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
       I.d[k] = F.d[k];
       I.padI[k] = F.padI[k];
     }
-    I.ncb = ((F.N + kColBlock - 1) / kColBlock);
-    I.pitch = F.pitchI;
+    I.pitch = 0;
     I.grid = F.grid;
     I.kern = F.kern;
     I.obs = F.obs;
     I.xcstride = F.N * F.N;
-    // band height and channels per pass: use the most threads that fit
-    int best_score = -1;
-    for (int cp = 2; cp >= 1; --cp)
-      for (int bo = F.N; bo >= 1; --bo) {
-        const int brows = bo + F.KS - 1;
-        const int fl = 2 * F.nplanes * brows * F.N + cp * F.nplanes * brows * F.pitchI +
-                       F.nplanes * F.KS * F.ksp;
-        if (fl * 4 + static_bytes > dev_smem) continue;
-        const int units = bo * I.ncb * cp;
+    I.cpass = D;
+    int dmin = F.d[0], dmax = F.d[0];
+    for (int p = 1; p < F.ss; ++p) {
+      dmin = std::min(dmin, F.d[p]);
+      dmax = std::max(dmax, F.d[p]);
+    }
+    I.R0 = dmax;
+    // Layout: per channel slot, ss^2 parity planes of brows rows x pitch
+    // floats (image rows with a top/bottom halo of the sub-kernel, columns
+    // with a zero right halo), then the sub-kernels.  Prefer the whole image
+    // in one band with as many channels per pass as fit; among column blocks
+    // of 16 and 20 pick the one that keeps the most of the 512 threads busy.
+    const int kern_floats = F.nplanes * F.KS * F.ksp;
+    const int avail = dev_smem - static_bytes - kern_floats * 4;
+    double best_score = -1.0;
+    for (int cb : {20, 16}) {
+      if (cb == 20 && F.KS > 15) continue;
+      const int ncbC = (F.N + cb - 1) / cb;
+      const int segn = (cb + F.KS - 1 + 3) & ~3;
+      int pitch = std::max(F.N + F.KS - 1, (ncbC - 1) * cb + segn);
+      pitch = (pitch + 3) & ~3;
+      if ((pitch / 4) % 2 == 0) pitch += 4;
+      // band height: the whole image when one channel's planes fit
+      int bo = F.N;
+      while (bo >= 1 && F.nplanes * (bo + F.KS + dmax - dmin) * pitch * 4 > avail) --bo;
+      if (bo < 1) continue;
+      const int brows = bo + F.KS + dmax - dmin;
+      const int set_bytes = F.nplanes * brows * pitch * 4;
+      const int cp_max = std::max(1, std::min(std::min(avail / set_bytes, D), 4));
+      for (int cp = 1; cp <= cp_max; ++cp) {
+        const int units = cp * ncbC * bo;
         const int rounds = (units + kThreads - 1) / kThreads;
-        const int nbands = (F.N + bo - 1) / bo;
-        // score: thread utilisation of the correlation and halo overhead
-        const double util = (double)units / (rounds * kThreads);
-        const double halo = (double)bo / brows;
-        const int score = (int)(1e6 * util * halo * (cp == 2 ? 1.0 : 0.9));
+        const double util = (double)cp * bo * F.N / ((double)rounds * kThreads * cb);
+        const double halo = (double)bo / std::min(brows, F.N);   // rows evaluated per output row
+        const double score = util * std::min(1.0, halo) * (1.0 + 0.02 * cp);
         if (score > best_score) {
           best_score = score;
+          I.CB = cb;
+          I.ncbC = ncbC;
+          I.pitch = pitch;
           I.Bo = bo;
-          I.CPn = cp;
           I.brows = brows;
-          I.nbands = nbands;
+          I.CPn = cp;
         }
-        break;   // the largest band for this cp
       }
+    }
     if (best_score < 0) {
       set_error("least squares: image %d does not fit in shared memory", i);
       delete L;
       return GL_ERR_UNSUPPORTED;
     }
-    // refine: among band heights that fit, pick the best utilisation
-    for (int bo = I.Bo; bo >= 4; --bo) {
-      const int units = bo * I.ncb * I.CPn;
-      const int rounds = (units + kThreads - 1) / kThreads;
-      const double util = (double)units / (rounds * kThreads);
-      const double halo = (double)bo / (bo + F.KS - 1);
-      const int score = (int)(1e6 * util * halo * (I.CPn == 2 ? 1.0 : 0.9));
-      if (score > best_score) {
-        best_score = score;
-        I.Bo = bo;
-        I.brows = bo + F.KS - 1;
-        I.nbands = (F.N + bo - 1) / bo;
-      }
+    I.nbands = (F.N + I.Bo - 1) / I.Bo;
+    I.plane_floats = I.brows * I.pitch;
+    I.offK = I.CPn * F.nplanes * I.plane_floats;
+    I.smem_floats = I.offK + kern_floats;
+    // the per-pixel loops divide indices below 2^21 through float reciprocals
+    if ((long long)F.nplanes * std::min(I.brows, F.N) * F.N >= (1 << 21)) {
+      set_error("least squares: image %d too large (%d px)", i, F.N);
+      delete L;
+      return GL_ERR_UNSUPPORTED;
     }
-    I.cpass = D;
-    I.offB = 0;
-    I.offP = 2 * F.nplanes * I.brows * F.N;
-    I.offP = (I.offP + 3) & ~3;
-    I.offK = I.offP + I.CPn * F.nplanes * I.brows * F.pitchI;
-    I.smem_floats = I.offK + F.nplanes * F.KS * F.ksp;
+    const size_t beta_n = (size_t)F.nplanes * std::min(I.brows, F.N) * F.N;
+    if (beta_n > beta_per_cta) beta_per_cta = beta_n;
     if (I.smem_floats * 4 > smem) smem = I.smem_floats * 4;
     if (F.N * F.N > maxP) maxP = F.N * F.N;
     if (I.nbands > max_bands) max_bands = I.nbands;
@@ -677,6 +711,9 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
   L->smem_bytes = smem;
   L->maxP = maxP;
   L->max_bands = max_bands;
+  L->beta_per_cta = beta_per_cta;
+  L->n_sm = 1;
+  cudaDeviceGetAttribute(&L->n_sm, cudaDevAttrMultiProcessorCount, plan->device);
   // error maps on the device
   size_t bytes = 0;
   for (int i = 0; i < plan->n_images; ++i) bytes += ((size_t)errs[i].size() * 4 + 255) / 256 * 256;
@@ -713,15 +750,22 @@ void lsq_destroy(gl_plan* plan) {
   plan->lsq = nullptr;
 }
 
+// CTAs of the basis kernel: one per work item, at most one per SM.
+static int basis_ctas(const LsqPlan* L, int bs) {
+  const long long items = (long long)bs * L->max_bands;
+  return (int)std::max(1LL, std::min(items, (long long)L->n_sm));
+}
+
 // Workspace: X [bs][D][maxP], G [bs][D][D], V [bs][D][D], h, r, ilam [bs][D],
-// ew [bs][maxP], status.
+// ew [bs][maxP], beta [basis CTAs][beta_per_cta] (float2), status.
 size_t lsq_workspace_bytes(const LsqPlan* L, int bs) {
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   const size_t X = (size_t)bs * L->D * L->maxP * 4;
   const size_t G = (size_t)bs * L->D * L->D * 4;
   const size_t h = (size_t)bs * L->D * 4;
   const size_t ew = (size_t)bs * L->maxP * 4;
-  return up(X) + 2 * up(G) + 3 * up(h) + up(ew) + 256;
+  const size_t beta = (size_t)basis_ctas(L, bs) * L->beta_per_cta * 8;
+  return up(X) + 2 * up(G) + 3 * up(h) + up(ew) + up(beta) + 256;
 }
 
 int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, float* work,
@@ -767,6 +811,10 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   base += up((size_t)bs * L->D * 4);
   float* ew = (float*)base;
   base += up((size_t)bs * L->maxP * 4);
+  const int n_basis = basis_ctas(L, bs);
+  a.beta = (float2*)base;
+  a.beta_stride = L->beta_per_cta;
+  base += up((size_t)n_basis * L->beta_per_cta * 8);
   int* status = (int*)base;
   float* co = coeffs;
   if (!co) {
@@ -775,10 +823,9 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   }
   int sms = 1;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
-  const int items = bs * L->max_bands;
   cudaMemsetAsync(status, 0, sizeof(int), stream);
   // basis stack, then G = A^T A on the tensor cores (3xTF32)
-  lsq_basis_kernel<<<items < sms ? items : sms, kThreads, L->smem_bytes, stream>>>(a);
+  lsq_basis_kernel<<<n_basis, kThreads, L->smem_bytes, stream>>>(a);
   int rc = launch_gram_tc(a, G, status, bs < 2 * sms ? bs : 2 * sms, stream);
   if (rc) return rc;
   // h = A^T b from the basis, c0 = pinv(G) h, then two refinement steps
@@ -864,10 +911,16 @@ extern "C" int gl_lstsq_noalloc(const gl_plan* plan, const float* x, const int* 
   const LsqPlan* L = (const LsqPlan*)plan->lsq;
   const size_t need = lsq_workspace_bytes(L, bs);
   if (need > kNoAllocScratchBytes) {
-    const size_t per = lsq_workspace_bytes(L, 1);
+    // the workspace grows with the batch: bisect for the largest batch that fits
+    int lo = 0, hi = bs;
+    while (hi - lo > 1) {
+      const int mid = lo + (hi - lo) / 2;
+      if (lsq_workspace_bytes(L, mid) <= kNoAllocScratchBytes) lo = mid;
+      else hi = mid;
+    }
     set_error("gl_lstsq_noalloc: %d chains need %zu bytes of scratch, more than its fixed %zu bytes "
-              "(at most %zu chains for this plan); split the batch or use gl_lstsq",
-              bs, need, kNoAllocScratchBytes, per ? kNoAllocScratchBytes / per : (size_t)0);
+              "(at most %d chains for this plan); split the batch or use gl_lstsq",
+              bs, need, kNoAllocScratchBytes, lo);
     return GL_ERR_INVALID;
   }
   void* scratch = nullptr;

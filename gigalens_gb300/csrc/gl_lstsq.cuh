@@ -24,14 +24,18 @@ struct LsqProfile {
 struct LsqImage {
   int N, ss, nplanes, KS, ksp;
   int d[kMaxPlanes], padI[kMaxPlanes];
-  int ncb, pitch;
-  int Bo;      // output rows per band
-  int CPn;     // channels per correlation pass
-  int brows;   // plane rows per band (Bo + KS - 1)
+  int pitch;          // plane row pitch in floats (a multiple of 4 with pitch / 4 odd)
+  int CB;             // output columns per correlation unit (16 or 20)
+  int ncbC;           // column blocks of CB columns
+  int Bo;             // output rows per band (N: the whole image in one band)
+  int CPn;            // channels per pass
+  int R0;             // max_p d[p]: shared-memory row 0 holds plane row i0 - R0
+  int brows;          // plane rows held per band: Bo + KS + R0 - min_p d[p]
   int nbands;
-  int cpass;   // number of channels (D)
-  int xcstride;   // floats between channels in X (N*N)
-  int offB, offP, offK, smem_floats;
+  int cpass;          // number of channels (D)
+  int xcstride;       // floats between channels in X (N*N)
+  int plane_floats;   // brows * pitch
+  int offK, smem_floats;
   const float* grid;
   const float* kern;
   const float* obs;
@@ -42,6 +46,8 @@ struct LsqArgs {
   int bs, d, D, n_images, n_prof, has_shear;
   int maxP, max_bands;
   size_t xstride;   // floats per sample in X
+  float2* beta;         // ray-traced source-plane coordinates, one slice per CTA
+  size_t beta_stride;   // float2 per slice
   LsqProfile prof[kMaxLsqProfiles];
   LsqChannel ch[kMaxLsqChannels];
   DevProfile epl, shear;
@@ -53,6 +59,8 @@ struct LsqArgs {
 
 struct LsqPlan {
   int D, n_prof, has_shear, maxP, max_bands, smem_bytes;
+  int n_sm;             // CTAs of the basis kernel at most (one per SM)
+  size_t beta_per_cta;  // float2 of the largest band's ray-traced coordinates
   LsqProfile prof[kMaxLsqProfiles];
   LsqChannel ch[kMaxLsqChannels];
   DevProfile epl, shear;

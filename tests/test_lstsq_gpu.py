@@ -58,7 +58,8 @@ def _obs(n, rng):
     return (ring + rng.normal(scale=0.1, size=(n, n))).astype(np.float32)
 
 
-@pytest.mark.parametrize("n,ss,k,n_max,ll", [(40, 2, 21, 4, False), (48, 2, 13, 8, False), (36, 1, 13, 3, True)])
+@pytest.mark.parametrize("n,ss,k,n_max,ll", [(40, 2, 21, 4, False), (48, 2, 13, 8, False), (36, 1, 13, 3, True),
+                                            (44, 2, 11, 5, True), (32, 1, 11, 3, False), (120, 2, 21, 2, False)])
 def test_lstsq_simulate_matches_oracle(n, ss, k, n_max, ll):
     from gigalens_gb300.cuda.model import BackwardProbModel
     from gigalens_gb300.cuda.simulator import LensSimulator
