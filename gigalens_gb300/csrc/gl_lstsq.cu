@@ -51,6 +51,35 @@ __device__ __forceinline__ float hermite_fn(int n, float u, const float* pref) {
   return h1 * pref[n];
 }
 
+// The same recursion for U independent arguments of one order n (the
+// basis kernel evaluates U pixels per thread so their chains interleave).
+template <int U>
+__device__ __forceinline__ void hermite_fn_n(int n, const float (&u)[U], float (&out)[U], const float* pref) {
+  float h0[U], h1[U];
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    h0[k] = 1.f;
+    h1[k] = 2.f * u[k];
+  }
+  if (n == 0) {
+#pragma unroll
+    for (int k = 0; k < U; ++k) out[k] = pref[0];
+    return;
+  }
+  for (int i = 2; i <= n; ++i) {
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const float h2 = 2.f * (u[k] * h1[k] - (float)(i - 1) * h0[k]);
+      h0[k] = h1[k];
+      h1[k] = h2;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < U; ++k) out[k] = h1[k] * pref[n];
+}
+
+constexpr int kEvalU = 4;   // pixels per thread and iteration in the channel evaluation
+
 struct LsqShared {
   float x[GL_MAX_PARAMS];
   float4 tab[kMaxTerms + 2];
@@ -215,46 +244,72 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
           float* pbase = sbase + pq * I.plane_floats + I.padI[q];
           const float2* bp = beta + (size_t)pq * per_plane;
           const float4* gp = grid + ((size_t)pq * I.N + Ya) * I.N;
+          // kEvalU pixels per thread: their loads and recursions interleave
           if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
             const float ib = 1.f / lpget(st.x, pr.col[0], 1.f);
             const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
-            for (int i = tid; i < per_plane; i += kThreads) {
-              float px, py;
-              if (src) {
-                const float2 bt = bp[i];
-                px = bt.x;
-                py = bt.y;
-              } else {
-                const float4 xy = __ldg(gp + i);
-                px = xy.x;
-                py = xy.y;
+            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * kThreads) {
+              float u[kEvalU], w[kEvalU];
+#pragma unroll
+              for (int k = 0; k < kEvalU; ++k) {
+                const int i = min(i0 + k * kThreads, per_plane - 1);
+                float px, py;
+                if (src) {
+                  const float2 bt = bp[i];
+                  px = bt.x;
+                  py = bt.y;
+                } else {
+                  const float4 xy = __ldg(gp + i);
+                  px = xy.x;
+                  py = xy.y;
+                }
+                u[k] = (px - cx) * ib;
+                w[k] = (py - cy) * ib;
               }
-              const float u = (px - cx) * ib, w = (py - cy) * ib;
-              const float fac = expf(-(u * u + w * w) / 2.f);
-              float val = fac * hermite_fn(ch.n1, u, pref) * hermite_fn(ch.n2, w, pref);
-              if (isnan(val)) val = 0.f;
-              const int r = small_div(i, inv_n);
-              pbase[r * I.pitch + (i - r * I.N)] = val;
+              float hu[kEvalU], hw[kEvalU];
+              hermite_fn_n<kEvalU>(ch.n1, u, hu, pref);
+              hermite_fn_n<kEvalU>(ch.n2, w, hw, pref);
+#pragma unroll
+              for (int k = 0; k < kEvalU; ++k) {
+                const int i = i0 + k * kThreads;
+                if (i < per_plane) {
+                  const float fac = expf(-(u[k] * u[k] + w[k] * w[k]) / 2.f);
+                  float val = fac * hu[k] * hw[k];
+                  if (isnan(val)) val = 0.f;
+                  const int r = small_div(i, inv_n);
+                  pbase[r * I.pitch + (i - r * I.N)] = val;
+                }
+              }
             }
           } else {              // unit-amplitude Sersic
             const SerC sc = sersic_consts(lpget(st.x, pr.col[0], 1.f), lpget(st.x, pr.col[1], 1.f),
                                           lpget(st.x, pr.col[2], 0.f), lpget(st.x, pr.col[3], 0.f),
                                           lpget(st.x, pr.col[4], 0.f), lpget(st.x, pr.col[5], 0.f), 1.f);
-            for (int i = tid; i < per_plane; i += kThreads) {
-              float px, py;
-              if (src) {
-                const float2 bt = bp[i];
-                px = bt.x;
-                py = bt.y;
-              } else {
-                const float4 xy = __ldg(gp + i);
-                px = xy.x;
-                py = xy.y;
+            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * kThreads) {
+              float px[kEvalU], py[kEvalU];
+#pragma unroll
+              for (int k = 0; k < kEvalU; ++k) {
+                const int i = min(i0 + k * kThreads, per_plane - 1);
+                if (src) {
+                  const float2 bt = bp[i];
+                  px[k] = bt.x;
+                  py[k] = bt.y;
+                } else {
+                  const float4 xy = __ldg(gp + i);
+                  px[k] = xy.x;
+                  py[k] = xy.y;
+                }
               }
-              float val = sersic_light(sc, px, py);
-              if (isnan(val)) val = 0.f;
-              const int r = small_div(i, inv_n);
-              pbase[r * I.pitch + (i - r * I.N)] = val;
+#pragma unroll
+              for (int k = 0; k < kEvalU; ++k) {
+                const int i = i0 + k * kThreads;
+                if (i < per_plane) {
+                  float val = sersic_light(sc, px[k], py[k]);
+                  if (isnan(val)) val = 0.f;
+                  const int r = small_div(i, inv_n);
+                  pbase[r * I.pitch + (i - r * I.N)] = val;
+                }
+              }
             }
           }
         }
