@@ -462,60 +462,74 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
 }
 
 // img = sum_c coeffs_c X_c; BackwardProbModel likelihood with the data error map.
-// Residual of the weighted least-squares problem from the basis itself (not
-// from G): ew_p = W_p^2 (y_p - sum_c X_cp c_c), the channel sum in float32
-// groups of 8 added in float64
-// (c = NULL: ew = W^2 y, whose projection is h = A^T b).
-__global__ void __launch_bounds__(256) lsq_resid_pix_kernel(const __grid_constant__ LsqArgs a,
-                                                            const float* __restrict__ coeffs,
-                                                            float* __restrict__ ew) {
+// Projected residual of the weighted least-squares problem, from the basis
+// itself (not from G), in one pass over X.  One block per sample; per chunk
+// of 256 pixels: (1) thread t forms e_p = W_p^2 (y_p - sum_c X_cp c_c) of
+// pixel p = chunk + t (the channel sum in float32 groups of 8 added in
+// float64) into shared memory; (2) warp w projects the chunk onto channels
+// w, w + 8, ...: r_c += sum_p X_cp e_p, lanes over pixels (coalesced, the
+// chunk's X is still in L1), float32 over a chunk's 8 pixels per lane and
+// float64 across chunks and lanes.  c = NULL gives e = W^2 y and r = h = A^T b.
+constexpr int kResidThreads = 256;
+constexpr int kResidChPerWarp = kMaxLsqChannels / (kResidThreads / 32);
+__global__ void __launch_bounds__(kResidThreads) lsq_resid_kernel(const __grid_constant__ LsqArgs a,
+                                                                  const float* __restrict__ coeffs,
+                                                                  float* __restrict__ r) {
+  __shared__ float cf[kMaxLsqChannels];
+  __shared__ float e_s[kResidThreads];
   const int D = a.D;
-  for (int b = blockIdx.y; b < a.bs; b += gridDim.y) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = blockIdx.x; b < a.bs; b += gridDim.x) {
     const int im = a.img_id ? a.img_id[b] : 0;
     if (im < 0 || im >= a.n_images) continue;
     const LsqImage& I = a.img[im];
     const int P = I.N * I.N;
     const float* Xb = a.X + (size_t)b * a.xstride;
-    const float* cb = coeffs ? coeffs + (size_t)b * D : nullptr;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
-      double m = 0.0;
-      if (cb)
-        for (int c0 = 0; c0 < D; c0 += 8) {   // float32 groups of 8 channels, float64 across groups
+    for (int c = threadIdx.x; c < D; c += kResidThreads) cf[c] = coeffs ? coeffs[(size_t)b * D + c] : 0.f;
+    double acc[kResidChPerWarp];
+#pragma unroll
+    for (int k = 0; k < kResidChPerWarp; ++k) acc[k] = 0.0;
+    __syncthreads();
+    for (int p0 = 0; p0 < P; p0 += kResidThreads) {
+      const int p = p0 + threadIdx.x;
+      float e = 0.f;
+      if (p < P) {
+        double m = 0.0;
+        if (coeffs)
+          for (int c0 = 0; c0 < D; c0 += 8) {
+            float g = 0.f;
+            for (int c = c0; c < min(D, c0 + 8); ++c) g = fmaf(Xb[(size_t)c * I.xcstride + p], cf[c], g);
+            m += (double)g;
+          }
+        const float w = 1.f / I.err[p];
+        e = (float)(((double)I.obs[p] - m) * (double)(w * w));
+      }
+      e_s[threadIdx.x] = e;
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kResidChPerWarp; ++k) {
+        const int c = warp + k * (kResidThreads / 32);
+        if (c < D) {
+          const float* xc = Xb + (size_t)c * I.xcstride + p0;
           float g = 0.f;
-          for (int c = c0; c < min(D, c0 + 8); ++c) g = fmaf(Xb[(size_t)c * I.xcstride + p], __ldg(cb + c), g);
-          m += (double)g;
+#pragma unroll
+          for (int j = 0; j < kResidThreads / 32; ++j) {
+            const int q = lane + 32 * j;
+            if (p0 + q < P) g = fmaf(xc[q], e_s[q], g);
+          }
+          acc[k] += (double)g;
         }
-      const float w = 1.f / I.err[p];
-      ew[(size_t)b * a.maxP + p] = (float)(((double)I.obs[p] - m) * (double)(w * w));
+      }
+      __syncthreads();
     }
-  }
-}
-
-// r_c = sum_p X_cp ew_p: one warp per (sample, channel), 32-term float32
-// partial sums combined in float64.
-__global__ void __launch_bounds__(256) lsq_resid_proj_kernel(const __grid_constant__ LsqArgs a,
-                                                             const float* __restrict__ ew,
-                                                             float* __restrict__ r) {
-  const int D = a.D;
-  const int lane = threadIdx.x & 31;
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int t = wid; t < a.bs * D; t += nw) {
-    const int b = t / D, c = t - b * D;
-    const int im = a.img_id ? a.img_id[b] : 0;
-    if (im < 0 || im >= a.n_images) continue;
-    const LsqImage& I = a.img[im];
-    const int P = I.N * I.N;
-    const float* x = a.X + (size_t)b * a.xstride + (size_t)c * I.xcstride;
-    const float* e = ew + (size_t)b * a.maxP;
-    double acc = 0.0;
-    for (int p0 = 0; p0 < P; p0 += 32 * 32) {
-      float s = 0.f;
-      for (int p = p0 + lane; p < min(P, p0 + 32 * 32); p += 32) s = fmaf(x[p], e[p], s);
-      acc += (double)s;
+#pragma unroll
+    for (int k = 0; k < kResidChPerWarp; ++k) {
+      const int c = warp + k * (kResidThreads / 32);
+      double v = acc[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0 && c < D) r[(size_t)b * D + c] = (float)v;
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) r[(size_t)b * D + c] = (float)acc;
   }
 }
 
@@ -812,15 +826,14 @@ static int basis_ctas(const LsqPlan* L, int bs) {
 }
 
 // Workspace: X [bs][D][maxP], G [bs][D][D], V [bs][D][D], h, r, ilam [bs][D],
-// ew [bs][maxP], beta [basis CTAs][beta_per_cta] (float2), status.
+// beta [basis CTAs][beta_per_cta] (float2), status.
 size_t lsq_workspace_bytes(const LsqPlan* L, int bs) {
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   const size_t X = (size_t)bs * L->D * L->maxP * 4;
   const size_t G = (size_t)bs * L->D * L->D * 4;
   const size_t h = (size_t)bs * L->D * 4;
-  const size_t ew = (size_t)bs * L->maxP * 4;
   const size_t beta = (size_t)basis_ctas(L, bs) * L->beta_per_cta * 8;
-  return up(X) + 2 * up(G) + 3 * up(h) + up(ew) + up(beta) + 256;
+  return up(X) + 2 * up(G) + 3 * up(h) + up(beta) + 256;
 }
 
 int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, float* work,
@@ -864,8 +877,6 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   base += up((size_t)bs * L->D * 4);
   float* ilam = (float*)base;
   base += up((size_t)bs * L->D * 4);
-  float* ew = (float*)base;
-  base += up((size_t)bs * L->maxP * 4);
   const int n_basis = basis_ctas(L, bs);
   a.beta = (float2*)base;
   a.beta_stride = L->beta_per_cta;
@@ -885,15 +896,12 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   if (rc) return rc;
   // h = A^T b from the basis, c0 = pinv(G) h, then two refinement steps
   // against the residual of the least-squares problem itself
-  const dim3 pix_grid((L->maxP + 255) / 256 < 8 ? (L->maxP + 255) / 256 : 8, bs < 65535 ? bs : 65535);
-  const int proj_blocks = (bs * L->D + 7) / 8 < 8 * sms ? (bs * L->D + 7) / 8 : 8 * sms;
-  lsq_resid_pix_kernel<<<pix_grid, 256, 0, stream>>>(a, nullptr, ew);
-  lsq_resid_proj_kernel<<<proj_blocks, 256, 0, stream>>>(a, ew, h);
+  const int resid_blocks = bs < 8 * sms ? bs : 8 * sms;
+  lsq_resid_kernel<<<resid_blocks, kResidThreads, 0, stream>>>(a, nullptr, h);
   lsq_solve_kernel<<<bs < 8 * sms ? bs : 8 * sms, 128, 0, stream>>>(bs, L->D, G, h, 1e-6f, co, 30, V, ilam,
                                                                   status);
   for (int it = 0; it < 2; ++it) {
-    lsq_resid_pix_kernel<<<pix_grid, 256, 0, stream>>>(a, co, ew);
-    lsq_resid_proj_kernel<<<proj_blocks, 256, 0, stream>>>(a, ew, r);
+    lsq_resid_kernel<<<resid_blocks, kResidThreads, 0, stream>>>(a, co, r);
     lsq_update_kernel<<<bs < 8 * sms ? bs : 8 * sms, 64, 0, stream>>>(bs, L->D, V, ilam, r, co);
   }
   if (img_out || logL || chi2)
