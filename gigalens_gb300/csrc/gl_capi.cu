@@ -297,15 +297,12 @@ static int build_image(const gl_image_desc& g, DevImage& I, HostImage& hi) {
   // shared-memory layout
   // The pitch covers the segments read by the fused kernel (kFusedCB columns
   // per unit, plus one when the transposed correlation of column parity 1
-  // starts one float past a 16-byte boundary: PSF sizes k = 3 mod 4 at ss = 2)
-  // and by the least-squares kernel (kColBlock columns per unit).
+  // starts one float past a 16-byte boundary: PSF sizes k = 3 mod 4 at ss = 2).
   const int max_shift = I.d[ss - 1] - I.d[0];
   I.ncb = ((N + kFusedCB - 1) / kFusedCB + 1) & ~1;
   I.units = N * I.ncb;
   const int seg_f = (kFusedCB + KS - 1 + max_shift + 3) & ~3;
-  const int seg_l = (kColBlock + KS - 1 + 3) & ~3;
-  const int ncb_l = (N + kColBlock - 1) / kColBlock;
-  int pitch = (int)align_up(std::max(kFusedCB * (I.ncb - 1) + seg_f, kColBlock * (ncb_l - 1) + seg_l), 4);
+  int pitch = (int)align_up(kFusedCB * (I.ncb - 1) + seg_f, 4);
   if ((pitch / 4) % 2 == 0) pitch += 4;
   for (int q = 0; q < ss; ++q) I.padI[q] = I.d[q];
   I.pitchI = pitch;

@@ -1,35 +1,33 @@
 // Register-blocked 1-D correlation rows: the building block of the
 // PSF + supersample-binning correlations (forward and transposed) of the
-// fused and least-squares kernels.  A parity plane row segment and one
-// sub-kernel row are held in registers; each thread produces CB adjacent
-// outputs (kFusedCB in the fused kernel, kColBlock in the least-squares one).
+// fused and least-squares kernels.  A parity plane row segment is held in
+// registers and the sub-kernel row is read four taps at a time (a broadcast
+// 16-byte load); each thread produces CB adjacent outputs (kFusedCB in the
+// fused kernel, 16 or 20 in the least-squares one).
 #pragma once
 #include "gl_internal.cuh"
 
 namespace gl {
 
 // ---------------------------------------------------------------- correlation
-// acc[c] += sum_l k[l] * seg[c + l]  (REV: k[KS-1-l]); seg and krow 16-byte aligned.
-// The segment is held in registers; the kernel row is read four taps at a
-// time (a broadcast 16-byte load), which keeps the live set near CB + SEGN.
-template <int KS, bool REV, int CB = kColBlock>
-__device__ __forceinline__ void corr_row(const float* __restrict__ seg,
-                                         const float* __restrict__ krow, float (&acc)[CB]) {
-  constexpr int SEGN = (CB + KS - 1 + 3) & ~3;
-  constexpr int NG = (KS + 3) / 4;   // 16-byte groups of the kernel row
-  float s[SEGN];
+// One row of corr_rows: acc[c] += sum_l k[l] * seg[c + l + SHIFT] with the
+// segment already in registers.
+template <int KS, bool REV, int CB, int SHIFT, int NV>
+__device__ __forceinline__ void corr_row_regs(const float4 (&v)[NV], const float* __restrict__ kr,
+                                              float (&acc)[CB]) {
+  constexpr int NG = (KS + 3) / 4;
+  float s[4 * NV];
 #pragma unroll
-  for (int i = 0; i < SEGN / 4; ++i) {
-    float4 t = reinterpret_cast<const float4*>(seg)[i];
-    s[4 * i] = t.x;
-    s[4 * i + 1] = t.y;
-    s[4 * i + 2] = t.z;
-    s[4 * i + 3] = t.w;
+  for (int i = 0; i < NV; ++i) {
+    s[4 * i] = v[i].x;
+    s[4 * i + 1] = v[i].y;
+    s[4 * i + 2] = v[i].z;
+    s[4 * i + 3] = v[i].w;
   }
 #pragma unroll
   for (int gi = 0; gi < NG; ++gi) {
     const int g = REV ? NG - 1 - gi : gi;
-    const float4 t = reinterpret_cast<const float4*>(krow)[g];
+    const float4 t = reinterpret_cast<const float4*>(kr)[g];
     const float kq[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
     for (int ei = 0; ei < 4; ++ei) {
@@ -38,7 +36,7 @@ __device__ __forceinline__ void corr_row(const float* __restrict__ seg,
       if (kidx < KS) {
         const int l = REV ? KS - 1 - kidx : kidx;
 #pragma unroll
-        for (int c = 0; c < CB; ++c) acc[c] = fmaf(kq[e], s[c + l], acc[c]);
+        for (int c = 0; c < CB; ++c) acc[c] = fmaf(kq[e], s[c + l + SHIFT], acc[c]);
       }
     }
   }
@@ -47,52 +45,31 @@ __device__ __forceinline__ void corr_row(const float* __restrict__ seg,
 // n consecutive rows: acc[c] += sum_r sum_l k_r[l] * seg_r[c + l + SHIFT],
 // with seg_r = seg + r * seg_pitch (16-byte aligned; SHIFT < 4 skips the
 // first floats of the aligned segment) and k_r = krow + r * k_step (REV: taps
-// reversed).  The next row's segment is loaded while the current one is
-// consumed.  The prefetch of row n (one past the last) must stay inside
-// shared memory; its values are not used.
+// reversed).  Two register buffers alternate: the next row's segment loads
+// while the current one is consumed, with no copies between them.  The
+// prefetch may read row n (one past the last), which must stay inside shared
+// memory; its values are not used.
 template <int KS, bool REV, int CB, int SHIFT = 0>
 __device__ __forceinline__ void corr_rows(const float* __restrict__ seg, int seg_pitch,
                                           const float* __restrict__ krow, int k_step, int n,
                                           float (&acc)[CB]) {
-  constexpr int SEGN = (CB + KS - 1 + SHIFT + 3) & ~3;
-  constexpr int NG = (KS + 3) / 4;
-  float4 cur[SEGN / 4];
+  constexpr int NV = ((CB + KS - 1 + SHIFT + 3) & ~3) / 4;
+  float4 a[NV], b[NV];
 #pragma unroll
-  for (int i = 0; i < SEGN / 4; ++i) cur[i] = reinterpret_cast<const float4*>(seg)[i];
-#pragma unroll 2
-  for (int r = 0; r < n; ++r) {
-    float4 nxt[SEGN / 4];
-    const float4* sn = reinterpret_cast<const float4*>(seg + (r + 1) * seg_pitch);
+  for (int i = 0; i < NV; ++i) a[i] = reinterpret_cast<const float4*>(seg)[i];
+  int r = 0;
+#pragma unroll 1
+  for (; r + 1 < n; r += 2) {
+    const float4* s1 = reinterpret_cast<const float4*>(seg + (r + 1) * seg_pitch);
 #pragma unroll
-    for (int i = 0; i < SEGN / 4; ++i) nxt[i] = sn[i];
-    float s[SEGN];
+    for (int i = 0; i < NV; ++i) b[i] = s1[i];
+    corr_row_regs<KS, REV, CB, SHIFT>(a, krow + r * k_step, acc);
+    const float4* s2 = reinterpret_cast<const float4*>(seg + (r + 2) * seg_pitch);
 #pragma unroll
-    for (int i = 0; i < SEGN / 4; ++i) {
-      s[4 * i] = cur[i].x;
-      s[4 * i + 1] = cur[i].y;
-      s[4 * i + 2] = cur[i].z;
-      s[4 * i + 3] = cur[i].w;
-    }
-    const float* kr = krow + r * k_step;
-#pragma unroll
-    for (int gi = 0; gi < NG; ++gi) {
-      const int g = REV ? NG - 1 - gi : gi;
-      const float4 t = reinterpret_cast<const float4*>(kr)[g];
-      const float kq[4] = {t.x, t.y, t.z, t.w};
-#pragma unroll
-      for (int ei = 0; ei < 4; ++ei) {
-        const int e = REV ? 3 - ei : ei;
-        const int kidx = 4 * g + e;
-        if (kidx < KS) {
-          const int l = REV ? KS - 1 - kidx : kidx;
-#pragma unroll
-          for (int c = 0; c < CB; ++c) acc[c] = fmaf(kq[e], s[c + l + SHIFT], acc[c]);
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < SEGN / 4; ++i) cur[i] = nxt[i];
+    for (int i = 0; i < NV; ++i) a[i] = s2[i];
+    corr_row_regs<KS, REV, CB, SHIFT>(b, krow + (r + 1) * k_step, acc);
   }
+  if (r < n) corr_row_regs<KS, REV, CB, SHIFT>(a, krow + r * k_step, acc);
 }
 
 // Sub-kernel sides 1..25: odd for every PSF at ss = 1 and for PSF sizes

@@ -9,7 +9,6 @@ namespace gl {
 
 constexpr int kThreads = 512;        // 16 warps: 4 per SM sub-partition, up to 128 registers
 constexpr int kWarps = kThreads / 32;
-constexpr int kColBlock = 8;         // output columns per thread, least-squares PSF correlation
 constexpr int kFusedCB = 16;         // output columns per thread, fused-kernel PSF correlation
 constexpr int kMaxTerms = 256;       // largest EPL iteration cap the fused kernel accepts
 constexpr int kMaxKS = 25;           // largest parity sub-kernel side
