@@ -37,22 +37,11 @@ __device__ __forceinline__ float lpget(const float* sx, int col, float dflt) {
   return col >= 0 ? sx[col] : dflt;
 }
 
-// Normalised Hermite function value phi_n(u) without the Gaussian:
-// H_n(u) / sqrt(2^n sqrt(pi) n!), recursion H_n = 2 (u H_{n-1} - (n-1) H_{n-2})
-// (tf/profiles/light/shapelets.py:47-48,77-85).
-__device__ __forceinline__ float hermite_fn(int n, float u, const float* pref) {
-  float h0 = 1.f, h1 = 2.f * u;
-  if (n == 0) return h0 * pref[0];
-  for (int i = 2; i <= n; ++i) {
-    const float h2 = 2.f * (u * h1 - (float)(i - 1) * h0);
-    h0 = h1;
-    h1 = h2;
-  }
-  return h1 * pref[n];
-}
-
-// The same recursion for U independent arguments of one order n (the
-// basis kernel evaluates U pixels per thread so their chains interleave).
+// Normalised Hermite function values phi_n(u) without the Gaussian,
+// H_n(u) / sqrt(2^n sqrt(pi) n!), by the recursion H_n = 2 (u H_{n-1} -
+// (n-1) H_{n-2}) (tf/profiles/light/shapelets.py:47-48,77-85), for U
+// independent arguments of one order n (the basis kernel evaluates U pixels
+// per thread so their chains interleave).
 template <int U>
 __device__ __forceinline__ void hermite_fn_n(int n, const float (&u)[U], float (&out)[U], const float* pref) {
   float h0[U], h1[U];
@@ -66,10 +55,16 @@ __device__ __forceinline__ void hermite_fn_n(int n, const float (&u)[U], float (
     for (int k = 0; k < U; ++k) out[k] = pref[0];
     return;
   }
+  // H_i = (2u) H_{i-1} - 2(i-1) H_{i-2}: the factor 2 distributed (exact in
+  // binary floating point), two operations per step
+  float tu[U];
+#pragma unroll
+  for (int k = 0; k < U; ++k) tu[k] = 2.f * u[k];
   for (int i = 2; i <= n; ++i) {
+    const float c2 = (float)(2 * (i - 1));
 #pragma unroll
     for (int k = 0; k < U; ++k) {
-      const float h2 = 2.f * (u[k] * h1[k] - (float)(i - 1) * h0[k]);
+      const float h2 = fmaf(tu[k], h1[k], -(c2 * h0[k]));
       h0[k] = h1[k];
       h1[k] = h2;
     }
