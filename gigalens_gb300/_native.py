@@ -10,7 +10,7 @@ import threading
 
 from . import _build
 
-GL_ABI_VERSION = 2   # include/gigalens_cuda.h
+GL_ABI_VERSION = 3   # include/gigalens_cuda.h
 
 GL_OK = 0
 GL_ERR_INVALID = -1
@@ -76,6 +76,7 @@ class gl_profile_desc(ctypes.Structure):
         ("niter", ctypes.c_int),
         ("use_lstsq", ctypes.c_int),
         ("col", ctypes.c_int * GL_MAX_PROFILE_PARAMS),
+        ("interpolate", ctypes.c_int),
     ]
 
 
@@ -156,7 +157,7 @@ SIGNATURES = [
     ("gl_epl_term_count", _i, [_vp, _vp, _i64, _i, _vp, _vp]),
     ("gl_adam_step", _i, [_vp, _vp, _vp, _vp, _i64, ctypes.c_float, ctypes.POINTER(gl_adam_cfg), _vp, _vp]),
     ("gl_probe_fp32_fma", _i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_double), _vp]),
-    ("gl_shapelets_eval", _i, [_i, _vp, _vp, _i64, _vp, _vp, _vp, _vp]),
+    ("gl_shapelets_eval", _i, [_i, _i, _vp, _vp, _i64, _vp, _vp, _vp, _vp]),
     ("gl_lstsq_workspace", _i, [_vp, _i, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_i)]),
     ("gl_lstsq", _i, [_vp, _vp, _vp, _i, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp]),
     ("gl_lstsq_noalloc", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),

@@ -185,6 +185,7 @@ static int resolve_generic(const gl_model_desc* m, bool lsq, GenArgs* g, DevProf
           return GL_ERR_UNSUPPORTED;
         }
         L.n_max = p.niter;
+        L.interp = p.interpolate ? 1 : 0;
         for (int k = 0; k < 3; ++k) L.col[k] = p.col[k];
         const int D = (p.niter + 1) * (p.niter + 2) / 2;
         if (ext) {
@@ -573,6 +574,11 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
     I.err = put(hi[i].err);
   }
   rc = cuda_check(cudaGetLastError(), "plan upload");
+  // the table of the interpolating shapelet profiles (Shapelets(interpolate=True))
+  for (int i = 0; i < model->n_profiles && !rc; ++i)
+    if (model->prof[i].type == GL_PROF_SHAPELETS && model->prof[i].interpolate && !plan->shp_tab)
+      rc = shapelet_table(plan->device, &plan->shp_tab);
+  plan->gen.shp_tab = plan->shp_tab;
   if (!rc && plan->fused_fits) rc = fused_kernel_prepare(plan->smem_bytes);
   if (!rc && lsq_model) {
     std::vector<std::vector<float>> errs(n_images);
@@ -863,13 +869,20 @@ int gl_profile_eval(int type, const float* x, const float* y, int64_t n, const f
   return launch_profile_eval(type, x, y, n, params, n_terms, out0, out1, (cudaStream_t)stream);
 }
 
-int gl_shapelets_eval(int n_max, const float* x, const float* y, int64_t n, const float* params,
-                      const float* amps, float* out, void* stream) {
-  if (n_max < 0 || n_max > 30 || n < 0 || (n > 0 && (!x || !y || !params || !out))) {
+int gl_shapelets_eval(int n_max, int interpolate, const float* x, const float* y, int64_t n,
+                      const float* params, const float* amps, float* out, void* stream) {
+  if (n_max < 0 || n_max >= kShpTabRows || n < 0 || (n > 0 && (!x || !y || !params || !out))) {
     set_error("gl_shapelets_eval: bad arguments");
     return GL_ERR_INVALID;
   }
-  return launch_shapelets_eval(n_max, x, y, n, params, amps, out, (cudaStream_t)stream);
+  const float* tab = nullptr;
+  if (interpolate) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int rc = shapelet_table(dev, &tab);
+    if (rc) return rc;
+  }
+  return launch_shapelets_eval(n_max, tab, x, y, n, params, amps, out, (cudaStream_t)stream);
 }
 
 int gl_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out,

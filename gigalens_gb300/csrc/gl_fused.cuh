@@ -641,8 +641,8 @@ static __device__ __noinline__ void gen_mass_reverse(const DevProfile& m, const 
 }
 
 // Value of light slot l at (X, Y).
-__device__ __forceinline__ float gen_light(const GenLight& L, int l, const SmemStatic& st, float X,
-                                           float Y) {
+__device__ __forceinline__ float gen_light(const GenLight& L, int l, const SmemStatic& st, const float* tab,
+                                           float X, float Y) {
   const float* sx = st.x;
   const int* c = L.col;
   switch (L.type) {
@@ -657,6 +657,7 @@ __device__ __forceinline__ float gen_light(const GenLight& L, int l, const SmemS
       const float beta = pget(sx, c[0], 1.f);
       const float u = (X - pget(sx, c[1], 0.f)) / beta, v = (Y - pget(sx, c[2], 0.f)) / beta;
       const float* amp = L.amp_ext ? st.amp + L.amp_idx : sx + (c[3] >= 0 ? c[3] : 0);
+      if (L.interp) return shapelets_sum_interp(u, v, L.n_max, amp, tab, nullptr, nullptr);
       return shapelets_sum(u, v, L.n_max, amp, st.pref, nullptr, nullptr);
     }
     default:
@@ -667,8 +668,8 @@ __device__ __forceinline__ float gen_light(const GenLight& L, int l, const SmemS
 // Reverse of light slot l at (X, Y) with image adjoint gi: parameter adjoints
 // into acc[0..9], evaluation-point adjoint into (Xb, Yb).
 static __device__ __noinline__ void gen_light_reverse(const GenLight& L, int l, const SmemStatic& st,
-                                                  float X, float Y, float gi, float* acc, float& Xb,
-                                                  float& Yb) {
+                                                  const float* tab, float X, float Y, float gi, float* acc,
+                                                  float& Xb, float& Yb) {
   const float* sx = st.x;
   const int* c = L.col;
   switch (L.type) {
@@ -710,7 +711,10 @@ static __device__ __noinline__ void gen_light_reverse(const GenLight& L, int l, 
       const float u = (X - pget(sx, c[1], 0.f)) / beta, v = (Y - pget(sx, c[2], 0.f)) / beta;
       const float* amp = L.amp_ext ? st.amp + L.amp_idx : sx + (c[3] >= 0 ? c[3] : 0);
       float du, dv;
-      shapelets_sum(u, v, L.n_max, amp, st.pref, &du, &dv);
+      if (L.interp)
+        shapelets_sum_interp(u, v, L.n_max, amp, tab, &du, &dv);
+      else
+        shapelets_sum(u, v, L.n_max, amp, st.pref, &du, &dv);
       const float ub = gi * du / beta, vb = gi * dv / beta;   // adjoints of X, Y
       acc[0] += -(ub * u + vb * v);                            // d/d beta
       acc[1] -= ub;
@@ -762,7 +766,7 @@ static __device__ void phase_pixels_forward_gen(const FusedArgs& a, const DevIma
     for (int l = 0; l < kGenLight; ++l)
       if (l < g.n_light) {
         const bool src = g.light[l].group == GL_GROUP_SOURCE;
-        img += gen_light(g.light[l], l, st, src ? bx : xy.x, src ? by : xy.y);
+        img += gen_light(g.light[l], l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y);
       }
     if (isnan(img)) img = 0.f;
     sm[__float_as_int(xy.z)] = img;
@@ -784,13 +788,24 @@ __host__ __device__ constexpr int shp_n1(int k) { return shp_order(k) - shp_n2(k
 // the warp leaves lane l with the sums of amplitudes l and 32 + l.  Every
 // lane of the warp calls it (g = 0 where a lane has no pixel).
 static __device__ __forceinline__ void shapelet_amp_grad(float g, float u, float v, int nmax,
-                                                         const float* pref, float& acc_lo,
-                                                         float& acc_hi) {
+                                                         const float* pref, const float* tab,
+                                                         float& acc_lo, float& acc_hi) {
   const int lane = threadIdx.x & 31;
   float pu[kMaxShapeletN + 1], pv[kMaxShapeletN + 1];
-  shapelet_phis(u, nmax, pref, pu);
-  shapelet_phis(v, nmax, pref, pv);
-  const float fg = g * expf(-(u * u + v * v) / 2.f);
+  float fg;
+  if (tab) {   // interpolate=True: the tabulated functions carry the Gaussian
+    const ShpLerp Lu = shp_lerp(u), Lv = shp_lerp(v);
+#pragma unroll
+    for (int k = 0; k <= kMaxShapeletN; ++k) {
+      pu[k] = k <= nmax ? shp_tab_value(tab, k, Lu) : 0.f;
+      pv[k] = k <= nmax ? shp_tab_value(tab, k, Lv) : 0.f;
+    }
+    fg = g;
+  } else {
+    shapelet_phis(u, nmax, pref, pu);
+    shapelet_phis(v, nmax, pref, pv);
+    fg = g * expf(-(u * u + v * v) / 2.f);
+  }
   const int D = (nmax + 1) * (nmax + 2) / 2;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
@@ -868,7 +883,7 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
     for (int l = 0; l < kGenLight; ++l)
       if (l < g.n_light) {
         const bool src = g.light[l].group == GL_GROUP_SOURCE;
-        img += gen_light(g.light[l], l, st, src ? bx : xy.x, src ? by : xy.y);
+        img += gen_light(g.light[l], l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y);
       }
     if (!isnan(img)) {   // the reference zeroes NaN pixels: no gradient flows
     if (as >= 0) {
@@ -886,7 +901,7 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
       if (l < g.n_light) {
         const bool src = g.light[l].group == GL_GROUP_SOURCE;
         float Xb, Yb;
-        gen_light_reverse(g.light[l], l, st, src ? bx : xy.x, src ? by : xy.y, gimg,
+        gen_light_reverse(g.light[l], l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y, gimg,
                           acc + G_LIGHT + 10 * l, Xb, Yb);
         if (src) {
           bxb += Xb;
@@ -908,7 +923,9 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
       }
     }   // !isnan(img)
     }   // px < total
-    if (as >= 0) shapelet_amp_grad(ga, su, sv, g.light[as].n_max, st.pref, amp_lo, amp_hi);
+    if (as >= 0)
+      shapelet_amp_grad(ga, su, sv, g.light[as].n_max, st.pref, g.light[as].interp ? g.shp_tab : nullptr,
+                        amp_lo, amp_hi);
   }
   // the EPL slot's accumulators
 #pragma unroll

@@ -15,6 +15,11 @@ constexpr int kMaxKS = 25;           // largest parity sub-kernel side
 constexpr int kMaxPlanes = 4;        // supersample <= 2 in the fused kernel
 constexpr int kRedSlots = 48;        // reduced quantities per sample
 constexpr int kMaxShapeletN = 9;     // shapelets n_max <= 9: at most 55 basis functions
+// Shapelets(interpolate=True): phi_n(t) exp(-t^2/2) tabulated at kShpTabN
+// points on [kShpTabLo, kShpTabHi] for n < kShpTabRows
+constexpr int kShpTabN = 6000;
+constexpr int kShpTabRows = 31;
+constexpr float kShpTabLo = -5.f, kShpTabHi = 5.f;
 constexpr int kGenMass = 2;          // general path: mass profiles besides SHEAR
 constexpr int kGenLight = 3;         // general path: light profiles
 constexpr int kMaxAmps = 64;         // general path: external amplitudes per sample
@@ -78,6 +83,7 @@ struct GenLight {
   int n_max;    // shapelets
   int amp_ext;  // amplitude(s) from the external per-sample vector (least-squares coefficients)
   int amp_idx;  // index of the (first) amplitude in that vector
+  int interp;   // shapelets: tabulated functions (interpolate=True)
   int col[GL_MAX_PROFILE_PARAMS];   // SERSIC_ELLIPSE / CORE_SERSIC / SHAPELETS canonical columns
 };
 
@@ -94,6 +100,7 @@ struct GenArgs {
   int unit_cf;                 // images without the conversion factor (least-squares images)
   int explicit_shapelets;      // shapelet profiles with amplitude parameters
   int amp_grad_slot;           // the light slot whose amplitude gradients are reduced, or -1
+  const float* shp_tab;        // shapelet table (interpolating profiles), or null
 };
 
 struct FusedArgs {
@@ -146,6 +153,7 @@ struct gl_plan {
   int cta_floats;           // floats per CTA in gscratch
   int n_cta;                // CTAs gscratch holds (the device's SM count)
   void* lsq;                // gl::LsqPlan of the least-squares path, or null
+  const float* shp_tab;     // shapelet table (interpolating shapelet profiles), or null
 };
 
 namespace gl {
@@ -156,8 +164,10 @@ int fused_static_smem_bytes();
 // implemented in gl_profile_eval.cu
 int launch_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,
                         const int* n_terms, float* out0, float* out1, cudaStream_t stream);
-int launch_shapelets_eval(int n_max, const float* x, const float* y, int64_t n, const float* params,
-                          const float* amps, float* out, cudaStream_t stream);
+int launch_shapelets_eval(int n_max, const float* tab, const float* x, const float* y, int64_t n,
+                          const float* params, const float* amps, float* out, cudaStream_t stream);
+// Device address of the shapelet table on `device` (filled on first use).
+int shapelet_table(int device, const float** out);
 int launch_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out,
                           cudaStream_t stream);
 int launch_bijector_forward(const DevPriorLeaf* leaves, int d, const float* z, int bs, float* x,

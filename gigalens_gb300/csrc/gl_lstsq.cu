@@ -28,6 +28,7 @@
 #include "gl_corr.cuh"
 #include "gl_internal.cuh"
 #include "gl_profiles.cuh"
+#include "gl_profiles_gen.cuh"
 #include "gl_lstsq.cuh"
 
 namespace gl {
@@ -240,7 +241,40 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
           const float2* bp = beta + (size_t)pq * per_plane;
           const float4* gp = grid + ((size_t)pq * I.N + Ya) * I.N;
           // kEvalU pixels per thread: their loads and recursions interleave
-          if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
+          if (ch.kind == 1 && pr.interp) {   // tabulated shapelet functions (interpolate=True)
+            const float beta_s = lpget(st.x, pr.col[0], 1.f);
+            const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
+            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * kThreads) {
+              float u[kEvalU], w[kEvalU];
+#pragma unroll
+              for (int k = 0; k < kEvalU; ++k) {
+                const int i = min(i0 + k * kThreads, per_plane - 1);
+                float px, py;
+                if (src) {
+                  const float2 bt = bp[i];
+                  px = bt.x;
+                  py = bt.y;
+                } else {
+                  const float4 xy = __ldg(gp + i);
+                  px = xy.x;
+                  py = xy.y;
+                }
+                u[k] = (px - cx) / beta_s;
+                w[k] = (py - cy) / beta_s;
+              }
+#pragma unroll
+              for (int k = 0; k < kEvalU; ++k) {
+                const int i = i0 + k * kThreads;
+                if (i < per_plane) {
+                  float val = shp_tab_value(a.shp_tab, ch.n1, shp_lerp(u[k])) *
+                              shp_tab_value(a.shp_tab, ch.n2, shp_lerp(w[k]));
+                  if (isnan(val)) val = 0.f;
+                  const int r = small_div(i, inv_n);
+                  pbase[r * I.pitch + (i - r * I.N)] = val;
+                }
+              }
+            }
+          } else if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
             const float ib = 1.f / lpget(st.x, pr.col[0], 1.f);
             const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
             for (int i0 = tid; i0 < per_plane; i0 += kEvalU * kThreads) {
@@ -627,6 +661,7 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
     LsqProfile& pr = L->prof[L->n_prof];
     pr.group = p.group;
     pr.type = p.type;
+    pr.interp = p.type == GL_PROF_SHAPELETS && p.interpolate ? 1 : 0;
     for (int k = 0; k < GL_MAX_PROFILE_PARAMS; ++k) pr.col[k] = -1;
     if (p.type == GL_PROF_SHAPELETS) {
       if (p.niter < 0 || p.niter > kMaxShapeletN) {
@@ -851,6 +886,7 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   for (int i = 0; i < kMaxLsqChannels; ++i) a.ch[i] = L->ch[i];
   a.epl = L->epl;
   a.shear = L->shear;
+  a.shp_tab = plan->shp_tab;
   a.has_shear = L->has_shear;
   for (int i = 0; i < plan->n_images; ++i) a.img[i] = L->img[i];
   a.x = x;

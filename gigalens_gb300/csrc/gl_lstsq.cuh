@@ -18,6 +18,7 @@ struct LsqChannel {
 
 struct LsqProfile {
   int type, group;
+  int interp;   // shapelets: tabulated functions (interpolate=True)
   int col[GL_MAX_PROFILE_PARAMS];  // SHAPELETS: beta, cx, cy; Sersic: SERSIC_ELLIPSE slots
 };
 
@@ -48,6 +49,7 @@ struct LsqArgs {
   size_t xstride;   // floats per sample in X
   float2* beta;         // ray-traced source-plane coordinates, one slice per CTA
   size_t beta_stride;   // float2 per slice
+  const float* shp_tab; // shapelet table (interpolating shapelet profiles), or null
   LsqProfile prof[kMaxLsqProfiles];
   LsqChannel ch[kMaxLsqChannels];
   DevProfile epl, shear;

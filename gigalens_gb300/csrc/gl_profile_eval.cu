@@ -2,6 +2,10 @@
 // API), the EPL term-count rule as a device reduction, and the unconstraining
 // bijector.  These are the non-fused entry points; the fused kernel inlines
 // the same arithmetic from gl_profiles.cuh.
+#include <cmath>
+#include <mutex>
+#include <vector>
+
 #include "gl_internal.cuh"
 #include "gl_profiles.cuh"
 #include "gl_profiles_gen.cuh"
@@ -101,9 +105,9 @@ int launch_profile_eval(int type, const float* x, const float* y, int64_t n, con
 }
 
 // Shapelets at n points: Hermite recursion per point, all orders at once.
-__global__ void shapelets_eval_kernel(int n_max, const float* __restrict__ x, const float* __restrict__ y,
-                                      int64_t n, const float* __restrict__ prm, const float* __restrict__ amps,
-                                      float* __restrict__ out) {
+__global__ void shapelets_eval_kernel(int n_max, const float* __restrict__ tab, const float* __restrict__ x,
+                                      const float* __restrict__ y, int64_t n, const float* __restrict__ prm,
+                                      const float* __restrict__ amps, float* __restrict__ out) {
   __shared__ float pref[32];
   if (threadIdx.x <= n_max) {
     double f = 1.0;
@@ -115,6 +119,25 @@ __global__ void shapelets_eval_kernel(int n_max, const float* __restrict__ x, co
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float beta = prm[i], cx = prm[n + i], cy = prm[2 * n + i];
     const float u = (x[i] - cx) / beta, v = (y[i] - cy) / beta;
+    if (tab) {   // interpolate=True: products of tabulated 1-D functions
+      const ShpLerp Lu = shp_lerp(u), Lv = shp_lerp(v);
+      float acc = 0.f;
+      int n1 = 0, n2 = 0;
+      for (int k = 0; k < D; ++k) {
+        const float bk = shp_tab_value(tab, n1, Lu) * shp_tab_value(tab, n2, Lv);
+        if (amps) acc = fmaf(amps[(int64_t)k * n + i], bk, acc);
+        else out[(int64_t)k * n + i] = bk;
+        if (n1 == 0) {
+          n1 = n2 + 1;
+          n2 = 0;
+        } else {
+          --n1;
+          ++n2;
+        }
+      }
+      if (amps) out[i] = acc;
+      continue;
+    }
     float hu[32], hv[32];
     hu[0] = 1.f;
     hv[0] = 1.f;
@@ -162,17 +185,65 @@ __global__ void epl_term_count_kernel(const float* __restrict__ e1, const float*
   }
 }
 
-int launch_shapelets_eval(int n_max, const float* x, const float* y, int64_t n, const float* params,
-                          const float* amps, float* out, cudaStream_t stream) {
+int launch_shapelets_eval(int n_max, const float* tab, const float* x, const float* y, int64_t n,
+                          const float* params, const float* amps, float* out, cudaStream_t stream) {
   if (n == 0) return GL_OK;
   int64_t blocks = (n + 255) / 256;
   if (blocks > 4096) blocks = 4096;
-  shapelets_eval_kernel<<<(int)blocks, 256, 0, stream>>>(n_max, x, y, n, params, amps, out);
+  shapelets_eval_kernel<<<(int)blocks, 256, 0, stream>>>(n_max, tab, x, y, n, params, amps, out);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error("shapelets launch: %s", cudaGetErrorString(e));
     return GL_ERR_CUDA;
   }
+  return GL_OK;
+}
+
+// ------------------------------------------------------------------ shapelet table
+// psi_n(x_i) = phi_n(x_i) e^{-x_i^2/2}, x_i = lo + i (hi - lo) / (N - 1), the
+// reference's tables of lenstronomy's 1-D shapelet functions
+// (tf/profiles/light/shapelets.py:37-38: phi_n on linspace(-5, 5, 6000),
+// stored as float32).  Computed in double with the normalised recurrence
+// psi_0 = pi^{-1/4} e^{-x^2/2}, psi_1 = sqrt(2) x psi_0,
+// psi_n = sqrt(2/n) x psi_{n-1} - sqrt((n-1)/n) psi_{n-2}, which equals
+// H_n(x) e^{-x^2/2} / sqrt(2^n sqrt(pi) n!) without its large intermediates.
+static __device__ float g_shp_table[kShpTabRows * kShpTabN];
+constexpr int kShpMaxDevices = 64;
+static const float* g_shp_addr[kShpMaxDevices];
+static std::mutex g_shp_mutex;
+
+int shapelet_table(int device, const float** out) {
+  if (device < 0 || device >= kShpMaxDevices) {
+    set_error("shapelet table: device %d out of range", device);
+    return GL_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_shp_mutex);
+  if (!g_shp_addr[device]) {
+    std::vector<float> host((size_t)kShpTabRows * kShpTabN);
+    const double pi = 3.14159265358979323846;
+    for (int i = 0; i < kShpTabN; ++i) {
+      const double xv = (double)kShpTabLo + (double)i * ((double)kShpTabHi - (double)kShpTabLo) / (kShpTabN - 1);
+      double p0 = std::pow(pi, -0.25) * std::exp(-0.5 * xv * xv);
+      double p1 = std::sqrt(2.0) * xv * p0;
+      host[i] = (float)p0;
+      host[kShpTabN + i] = (float)p1;
+      for (int k = 2; k < kShpTabRows; ++k) {
+        const double p2 = std::sqrt(2.0 / k) * xv * p1 - std::sqrt((k - 1.0) / k) * p0;
+        host[(size_t)k * kShpTabN + i] = (float)p2;
+        p0 = p1;
+        p1 = p2;
+      }
+    }
+    cudaError_t e = cudaMemcpyToSymbol(g_shp_table, host.data(), host.size() * sizeof(float));
+    void* p = nullptr;
+    if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_shp_table);
+    if (e != cudaSuccess || !p) {
+      set_error("shapelet table: %s", cudaGetErrorString(e));
+      return GL_ERR_CUDA;
+    }
+    g_shp_addr[device] = (const float*)p;
+  }
+  *out = g_shp_addr[device];
   return GL_OK;
 }
 

@@ -9,7 +9,8 @@
 //               reference's grouping kept as it is: the core term
 //               (1 + (Rb/R)^alpha)^(gamma/alpha) times
 //               exp(-bn ((R^alpha + Rb^alpha) / R_sersic^alpha / (alpha n)) - 1)
-//   Shapelets   gigalens/tf/profiles/light/shapelets.py:66-85 (interpolate=False)
+//   Shapelets   gigalens/tf/profiles/light/shapelets.py:53-85 (interpolate=False: the
+//               Hermite recursion; True: the tabulated functions)
 #pragma once
 #include "gl_dual.cuh"
 
@@ -149,6 +150,88 @@ __device__ __forceinline__ void shapelet_phis(float t, int nmax, const float* pr
       ph[k] = 0.f;
     }
   }
+}
+
+// Tabulated shapelet functions (Shapelets(interpolate=True),
+// tf/profiles/light/shapelets.py:37-38,55-60): psi_n(t) = phi_n(t) e^{-t^2/2}
+// at kShpTabN points on [kShpTabLo, kShpTabHi], row n of `tab`, linearly
+// interpolated as tfp.math.interp_regular_1d_grid does -- fractional index
+// (t - lo) / (hi - lo) (N - 1) clipped to the grid, the bracket [i0, i0 + 1]
+// (the last bracket for the top point), value w y1 + (1 - w) y0 -- with 0
+// outside [lo, hi] and NaN for NaN t.  The slope d psi / dt is the bracket's
+// (y1 - y0) (N - 1) / (hi - lo), the derivative of that interpolant.
+struct ShpLerp {
+  int i0, i1;
+  float w;
+  int state;   // 0 inside, 1 outside (value 0), 2 NaN
+};
+__device__ __forceinline__ ShpLerp shp_lerp(float t) {
+  ShpLerp L;
+  L.state = isnan(t) ? 2 : ((t >= kShpTabLo && t <= kShpTabHi) ? 0 : 1);
+  float fi = (t - kShpTabLo) / (kShpTabHi - kShpTabLo) * (float)(kShpTabN - 1);
+  fi = fminf(fmaxf(fi, 0.f), (float)(kShpTabN - 1));   // a NaN index becomes 0
+  float ib = floorf(fi);
+  const float ia = fminf(ib + 1.f, (float)(kShpTabN - 1));
+  ib = fmaxf(ia - 1.f, 0.f);
+  L.w = fi - ib;
+  L.i0 = (int)ib;
+  L.i1 = (int)ia;
+  return L;
+}
+__device__ __forceinline__ float shp_tab_value(const float* __restrict__ tab, int n, const ShpLerp& L) {
+  if (L.state == 2) return __int_as_float(0x7fc00000);
+  if (L.state == 1) return 0.f;
+  const float* r = tab + n * kShpTabN;
+  const float y0 = __ldg(r + L.i0), y1 = __ldg(r + L.i1);
+  return L.w * y1 + (1.f - L.w) * y0;
+}
+__device__ __forceinline__ void shp_tab_value_slope(const float* __restrict__ tab, int n, const ShpLerp& L,
+                                                    float& val, float& slope) {
+  if (L.state != 0) {
+    val = slope = L.state == 2 ? __int_as_float(0x7fc00000) : 0.f;
+    return;
+  }
+  const float* r = tab + n * kShpTabN;
+  const float y0 = __ldg(r + L.i0), y1 = __ldg(r + L.i1);
+  val = L.w * y1 + (1.f - L.w) * y0;
+  slope = (y1 - y0) * ((float)(kShpTabN - 1) / (kShpTabHi - kShpTabLo));
+}
+
+// sum_k amp_k psi_n1(u) psi_n2(v) from the table, and its u, v partials.
+__device__ __forceinline__ float shapelets_sum_interp(float u, float v, int nmax, const float* amp,
+                                                      const float* __restrict__ tab, float* du, float* dv) {
+  float pu[kMaxShapeletN + 1], pv[kMaxShapeletN + 1], qu[kMaxShapeletN + 1], qv[kMaxShapeletN + 1];
+  const ShpLerp Lu = shp_lerp(u), Lv = shp_lerp(v);
+#pragma unroll
+  for (int k = 0; k <= kMaxShapeletN; ++k) {
+    if (k <= nmax) {
+      shp_tab_value_slope(tab, k, Lu, pu[k], qu[k]);
+      shp_tab_value_slope(tab, k, Lv, pv[k], qv[k]);
+    } else {
+      pu[k] = pv[k] = qu[k] = qv[k] = 0.f;
+    }
+  }
+  float s = 0.f, su = 0.f, sv = 0.f;
+#pragma unroll
+  for (int m = 0; m <= kMaxShapeletN; ++m) {
+    if (m <= nmax) {
+#pragma unroll
+      for (int j = 0; j <= m; ++j) {
+        const int n1 = m - j, n2 = j;
+        const float c = amp[m * (m + 1) / 2 + j];
+        s = fmaf(c, pu[n1] * pv[n2], s);
+        if (du) {
+          su = fmaf(c, qu[n1] * pv[n2], su);
+          sv = fmaf(c, pu[n1] * qv[n2], sv);
+        }
+      }
+    }
+  }
+  if (du) {
+    *du = su;
+    *dv = sv;
+  }
+  return s;
 }
 
 // Value of sum_k amp_k e^{-(u^2+v^2)/2} phi_n1(u) phi_n2(v) (k in the

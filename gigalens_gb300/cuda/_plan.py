@@ -67,6 +67,7 @@ class ModelLayout:
                 pd.group = gid
                 pd.niter = int(getattr(prof, "niter", getattr(prof, "n_max", 0)) or 0)
                 pd.use_lstsq = int(bool(getattr(prof, "use_lstsq", False)))
+                pd.interpolate = int(kind == "SHAPELETS" and bool(getattr(prof, "interpolate", False)))
                 for i in range(N.GL_MAX_PROFILE_PARAMS):
                     pd.col[i] = -1
                 for i, name in enumerate(N.CANONICAL_PARAMS[kind]):

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GL_ABI_VERSION 2
+#define GL_ABI_VERSION 3
 
 /* ---- error codes ---------------------------------------------------- */
 #define GL_OK 0
@@ -94,6 +94,12 @@ typedef struct {
                                       SHAPELETS: n_max                     */
   int use_lstsq;                   /* light: unit amplitude, solved linearly */
   int col[GL_MAX_PROFILE_PARAMS];  /* flat-vector column of each parameter */
+  int interpolate;                 /* SHAPELETS: Shapelets(interpolate=True),
+                                      the 1-D functions phi_n(t) exp(-t^2/2)
+                                      tabulated at 6000 points on [-5, 5]
+                                      and interpolated linearly, 0 outside
+                                      (tf/profiles/light/shapelets.py:37-38,
+                                      55-60); 0: exact Hermite recursion    */
 } gl_profile_desc;
 
 typedef struct {
@@ -196,12 +202,14 @@ int gl_bijector_forward(const gl_plan* plan, const float* z, int bs, float* x, v
  * (tf/profiles/mass/*.py deriv, tf/profiles/light/sersic.py light.)        */
 int gl_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,
                     const int* n_terms, float* out0, float* out1, void* stream);
-/* Shapelets.light (tf/profiles/light/shapelets.py:53-85, interpolate=False):
- * params [3, n] = (beta, center_x, center_y) per point.  amps [D, n] with
+/* Shapelets.light (tf/profiles/light/shapelets.py:53-85): params [3, n] =
+ * (beta, center_x, center_y) per point.  amps [D, n] with
  * D = (n_max+1)(n_max+2)/2 gives out [n] = sum_k amps_k basis_k; amps NULL
- * gives the unit-amplitude basis stack out [D, n] (use_lstsq).             */
-int gl_shapelets_eval(int n_max, const float* x, const float* y, int64_t n, const float* params,
-                      const float* amps, float* out, void* stream);
+ * gives the unit-amplitude basis stack out [D, n] (use_lstsq).
+ * interpolate: 1 for the tabulated functions (interpolate=True), 0 for the
+ * exact recursion (interpolate=False).                                     */
+int gl_shapelets_eval(int n_max, int interpolate, const float* x, const float* y, int64_t n,
+                      const float* params, const float* amps, float* out, void* stream);
 /* tf/profiles/mass/epl.py:41,51-56: K = min(cap, #{i=1,2,..: i < log(1e-12)/log(max f)+2})
  * over n ellipticity pairs; writes the int K to *k_out (device).           */
 int gl_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int* k_out, void* stream);
@@ -209,7 +217,7 @@ int gl_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, int*
 /* ---- linear amplitudes (least squares) -------------------------------- */
 /* LensSimulator.lstsq_simulate (tf/simulator.py:99-165) for a plan whose
  * light profiles all have use_lstsq (unit-amplitude Sersic, Shapelets with
- * interpolate=False): basis stack -> PSF + binning -> weighted normal
+ * either interpolate setting): basis stack -> PSF + binning -> weighted normal
  * equations G = X^T W^2 X, h = X^T W^2 y (W = 1/err_map) -> coeffs =
  * pinv(G, rcond=1e-6) h -> img = sum_c coeffs_c X_c (no conversion factor,
  * as the reference) -> BackwardProbModel likelihood with the error map

@@ -239,19 +239,65 @@ def shapelet_phi_n(u, n_max: int):
     return out
 
 
-def shapelets_basis(x, y, center_x, center_y, beta, n_max: int):
-    """Unit-amplitude basis stack ``(D, ...)``, ``tf/profiles/light/shapelets.py:66-72``."""
+SHAPELET_TABLE_N = 6000
+SHAPELET_TABLE_LO, SHAPELET_TABLE_HI = -5.0, 5.0
+
+
+def shapelet_table(n_max: int) -> np.ndarray:
+    """The reference's tabulated 1-D shapelet functions
+    (``tf/profiles/light/shapelets.py:37-38``: lenstronomy's
+    ``phi_n(n, linspace(-5, 5, 6000))`` stored as float32).  lenstronomy is
+    not installed; its ``phi_n`` is the published 1-D shapelet function
+    ``H_n(t) exp(-t^2/2) / sqrt(2^n sqrt(pi) n!)`` (Refregier 2003), evaluated
+    here in float64 from the Hermite recursion and rounded to float32."""
+    t = np.linspace(SHAPELET_TABLE_LO, SHAPELET_TABLE_HI, SHAPELET_TABLE_N)
+    H = [np.ones_like(t), 2 * t]
+    for i in range(2, n_max + 1):
+        H.append(2 * (t * H[-1] - (i - 1) * H[-2]))
+    rows = [H[n] * np.exp(-t ** 2 / 2) / math.sqrt(2 ** n * math.sqrt(math.pi) * math.factorial(n))
+            for n in range(n_max + 1)]
+    return np.asarray(rows).astype(np.float32)
+
+
+def interp_regular_1d(x, table_row):
+    """``tfp.math.interp_regular_1d_grid(x, -5, 5, row, fill_value_below=0,
+    fill_value_above=0)`` (``tf/profiles/light/shapelets.py:57-60``): the
+    fractional index ``(x - lo) / (hi - lo) (N - 1)`` clipped to the grid, the
+    bracket below it (the last bracket for the top point), ``w y1 + (1 - w) y0``;
+    0 outside [lo, hi], NaN for NaN x.  Differentiable in x (the bracket's
+    slope), as TensorFlow's gradient of that interpolation."""
+    y = torch.as_tensor(table_row, dtype=x.dtype)
+    n = y.numel()
+    fi = (x - SHAPELET_TABLE_LO) / (SHAPELET_TABLE_HI - SHAPELET_TABLE_LO) * (n - 1)
+    fi = torch.nan_to_num(fi, nan=0.0).clamp(0, n - 1)
+    ib = torch.floor(fi.detach())
+    ia = torch.clamp(ib + 1, max=n - 1)
+    ib = torch.clamp(ia - 1, min=0)
+    w = fi - ib
+    out = w * y[ia.long()] + (1 - w) * y[ib.long()]
+    out = torch.where((x < SHAPELET_TABLE_LO) | (x > SHAPELET_TABLE_HI), torch.zeros_like(out), out)
+    return torch.where(torch.isnan(x), x, out)
+
+
+def shapelets_basis(x, y, center_x, center_y, beta, n_max: int, interpolate: bool = False):
+    """Unit-amplitude basis stack ``(D, ...)``, ``tf/profiles/light/shapelets.py:53-72``;
+    ``interpolate``: products of the tabulated 1-D functions."""
     u = (x - center_x) / beta
     v = (y - center_y) / beta
+    N1, N2 = shapelet_orders(n_max)
+    if interpolate:
+        tab = shapelet_table(n_max)
+        TU = [interp_regular_1d(u, tab[n]) for n in range(n_max + 1)]
+        TV = [interp_regular_1d(v, tab[n]) for n in range(n_max + 1)]
+        return torch.stack([TU[a] * TV[b] for a, b in zip(N1, N2)], dim=0)
     XX, YY = shapelet_phi_n(u, n_max), shapelet_phi_n(v, n_max)
     fac = torch.exp(-(u ** 2 + v ** 2) / 2)
-    N1, N2 = shapelet_orders(n_max)
     return torch.stack([fac * XX[a] * YY[b] for a, b in zip(N1, N2)], dim=0)
 
 
-def shapelets_light(x, y, center_x, center_y, beta, amps: Sequence, n_max: int):
-    """Amplitude-weighted sum, ``tf/profiles/light/shapelets.py:73-75``."""
-    basis = shapelets_basis(x, y, center_x, center_y, beta, n_max)
+def shapelets_light(x, y, center_x, center_y, beta, amps: Sequence, n_max: int, interpolate: bool = False):
+    """Amplitude-weighted sum, ``tf/profiles/light/shapelets.py:61-64,73-75``."""
+    basis = shapelets_basis(x, y, center_x, center_y, beta, n_max, interpolate)
     out = torch.zeros_like(basis[0])
     for k, a in enumerate(amps):
         out = out + a * basis[k]
@@ -295,12 +341,13 @@ def _light(kind, opts, x, y, p, lstsq=False):
         return out[None] if lstsq else out
     if kind == "SHAPELETS":
         n_max = opts["n_max"]
+        interp = bool(opts.get("interpolate", False))
         if lstsq:
-            return shapelets_basis(x, y, p["center_x"], p["center_y"], p["beta"], n_max)
+            return shapelets_basis(x, y, p["center_x"], p["center_y"], p["beta"], n_max, interp)
         D = (n_max + 1) * (n_max + 2) // 2
         width = len(str(D))
         amps = [p[f"amp{str(i).zfill(width)}"] for i in range(D)]
-        return shapelets_light(x, y, p["center_x"], p["center_y"], p["beta"], amps, n_max)
+        return shapelets_light(x, y, p["center_x"], p["center_y"], p["beta"], amps, n_max, interp)
     raise ValueError(kind)
 
 

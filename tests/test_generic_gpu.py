@@ -89,11 +89,13 @@ def _model(name):
                                                 center_y=tfd.Normal(-0.1, 0.1),
                                                 Ie=tfd.LogNormal(math.log(80.0), 0.3)))]),
         ])
-    elif name == "sis_shapelets_explicit":
+    elif name in ("sis_shapelets_explicit", "sis_shapelets_interp"):
         n_max = 3
-        sh = shapelets.Shapelets(n_max, use_lstsq=False, interpolate=False)
+        interp = name == "sis_shapelets_interp"
+        sh = shapelets.Shapelets(n_max, use_lstsq=False, interpolate=interp)
         phys = PhysicalModel([sis.SIS()], [], [sh])
-        om = dict(lenses=[("SIS", {})], lens_light=[], source_light=[("SHAPELETS", {"n_max": n_max})])
+        om = dict(lenses=[("SIS", {})], lens_light=[],
+                  source_light=[("SHAPELETS", {"n_max": n_max, "interpolate": interp})])
         amps = {a: tfd.Normal(0.0, 20.0) for a in sh._amp_names}
         prior = tfd.JointDistributionSequential([
             tfd.JointDistributionSequential([
@@ -126,7 +128,8 @@ def _setup(name, num_pix=40, ss=2, k=13, bs=6, seed=0):
                 x_struct=prior.sample(bs, seed=seed))
 
 
-GRAD_CASES = ["sie_shear_coresersic_se", "epl_tnfw_shear_se", "sis_se_two_sources", "sis_shapelets_explicit"]
+GRAD_CASES = ["sie_shear_coresersic_se", "epl_tnfw_shear_se", "sis_se_two_sources", "sis_shapelets_explicit",
+              "sis_shapelets_interp"]
 
 
 @pytest.mark.parametrize("name", GRAD_CASES)

@@ -128,30 +128,71 @@ def test_lstsq_uneven_batch_two_images():
 
 
 @pytest.mark.parametrize("use_lstsq", [True, False])
-def test_shapelets_light_api(use_lstsq):
+@pytest.mark.parametrize("interpolate", [False, True])
+@pytest.mark.parametrize("scale", [1.0, 4.0])
+def test_shapelets_light_api(use_lstsq, interpolate, scale):
     """``tests/test_profiles.py:35-47`` of the reference: n_max=5, beta=1,
-    5x5 N(0,1) points, rtol 1e-5 / atol 1e-4 (here against the oracle)."""
+    5x5 N(0,1) points, rtol 1e-5 / atol 1e-4 (here against the oracle of
+    the same mode); scale 4 spreads the points past the table's [-5, 5]."""
     from gigalens_gb300.cuda.profiles.light.shapelets import Shapelets
 
     rng = np.random.default_rng(0)
-    shp = Shapelets(n_max=5, use_lstsq=use_lstsq, interpolate=False)
-    x = rng.normal(size=(5, 5, 1)).astype(np.float32)
-    y = rng.normal(size=(5, 5, 1)).astype(np.float32)
+    shp = Shapelets(n_max=5, use_lstsq=use_lstsq, interpolate=interpolate)
+    x = (scale * rng.normal(size=(5, 5, 1))).astype(np.float32)
+    y = (scale * rng.normal(size=(5, 5, 1))).astype(np.float32)
     D = torch.float64
     if use_lstsq:
         got = shp.light(torch.tensor(x).cuda(), torch.tensor(y).cuda(), center_x=0.0, center_y=0.0, beta=1.0)
         ref = O.shapelets_basis(torch.tensor(x, dtype=D), torch.tensor(y, dtype=D), torch.tensor(0.0, dtype=D),
-                                torch.tensor(0.0, dtype=D), torch.tensor(1.0, dtype=D), 5)
+                                torch.tensor(0.0, dtype=D), torch.tensor(1.0, dtype=D), 5, interpolate)
     else:
         amps = rng.normal(size=(shp.n_layers, 1)).astype(np.float32)
         amp = {k: torch.tensor(a) for k, a in zip(shp._amp_names, amps)}
         got = shp.light(torch.tensor(x).cuda(), torch.tensor(y).cuda(), center_x=0.0, center_y=0.0, beta=1.0, **amp)
         ref = O.shapelets_light(torch.tensor(x, dtype=D), torch.tensor(y, dtype=D), torch.tensor(0.0, dtype=D),
                                 torch.tensor(0.0, dtype=D), torch.tensor(1.0, dtype=D),
-                                [torch.tensor(a, dtype=D) for a in amps], 5)
+                                [torch.tensor(a, dtype=D) for a in amps], 5, interpolate)
     g = got.double().cpu().numpy().reshape(ref.shape)
     assert np.allclose(g, ref.numpy(), rtol=1e-5, atol=1e-4)
     assert np.abs(g - ref.numpy()).max() < 1e-6
+    if interpolate and scale > 1:
+        # the table's cut: points with |x| > 5 give exactly zero
+        outside = (np.abs(x) > 5) | (np.abs(y) > 5)
+        assert outside.any() and np.all(g.reshape(-1, *x.shape)[..., outside] == 0.0)
+
+
+def test_lstsq_interpolated_shapelets_match_oracle():
+    """lstsq_simulate with the reference's default Shapelets(interpolate=True):
+    the basis is the tabulated functions, cut to zero past 5 beta."""
+    from gigalens_gb300.cuda.model import BackwardProbModel
+    from gigalens_gb300.cuda.profiles.light import sersic, shapelets
+    from gigalens_gb300.cuda.profiles.mass import epl, shear
+    from gigalens_gb300.cuda.simulator import LensSimulator
+
+    n, ss, k, n_max = 40, 2, 21, 6
+    prior = shapelet_prior(n_max, True)
+    phys = PhysicalModel([epl.EPL(50), shear.Shear()], [sersic.SersicEllipse(use_lstsq=True)],
+                         [shapelets.Shapelets(n_max, use_lstsq=True, interpolate=True)])
+    omodel = dict(lenses=[("EPL", {"niter": 50}), ("SHEAR", {})], lens_light=[("SERSIC_ELLIPSE", {})],
+                  source_light=[("SHAPELETS", {"n_max": n_max, "interpolate": True})])
+    ksub = gaussian_psf(0.1, 0.08 / ss, k)
+    cfg = SimulatorConfig(delta_pix=0.08, num_pix=n, supersample=ss, kernel_supersampled=ksub)
+    obs = _obs(n, np.random.default_rng(n))
+    pm = BackwardProbModel(prior, obs, background_rms=0.1, exp_time=200.0)
+    bs = 6
+    sim = LensSimulator(phys, cfg, bs=bs)
+    xs = prior.sample(bs, seed=1)
+    img = sim.lstsq_simulate(xs, pm.observed_numpy, pm.err_numpy)
+    ocfg = O.SimConfig(0.08, n, ss, ksub.astype(np.float64))
+    ox = [[{kk: v.double() for kk, v in d.items()} for d in g] for g in xs]
+    ref = O.lstsq_simulate(omodel, ocfg, ox, obs.astype(np.float64), pm.err_numpy.astype(np.float64))
+    got = img.double().cpu().reshape(ref.shape)
+    scale = ref.abs().amax(dim=(-2, -1), keepdim=True)
+    assert float(((got - ref).abs() / scale).max()) < 2e-4
+    # the cut matters at these scales: the exact basis gives another fit
+    ox_exact = dict(omodel, source_light=[("SHAPELETS", {"n_max": n_max})])
+    ref_exact = O.lstsq_simulate(ox_exact, ocfg, ox, obs.astype(np.float64), pm.err_numpy.astype(np.float64))
+    assert float(((ref_exact - ref).abs() / scale).max()) > 1e-3
 
 
 def test_tensor_core_gram_accuracy():

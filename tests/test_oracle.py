@@ -188,3 +188,35 @@ def test_flat_layout_explicit_shapelets():
     assert names[:3] == ["center_x", "center_y", "theta_E"]
     assert names[3:13] == ["amp%02d" % i for i in range(10)]
     assert names[13:] == ["beta", "center_x", "center_y"]
+
+
+def test_interpolated_shapelets_match_exact_inside_the_table():
+    """Shapelets(interpolate=True) against interpolate=False with the
+    reference's own test (tests/test_profiles.py:35-47: n_max=5, beta=1,
+    5x5 N(0,1) points, rtol 1e-5 / atol 1e-4, both modes against
+    lenstronomy's function, which is the exact one here)."""
+    rng = np.random.default_rng(0)
+    x = torch.tensor(rng.normal(size=(5, 5)), dtype=torch.float64)
+    y = torch.tensor(rng.normal(size=(5, 5)), dtype=torch.float64)
+    z = torch.tensor(0.0, dtype=torch.float64)
+    one = torch.tensor(1.0, dtype=torch.float64)
+    amps = [torch.tensor(a, dtype=torch.float64) for a in rng.normal(size=21)]
+    a = O.shapelets_light(x, y, z, z, one, amps, 5, interpolate=True)
+    b = O.shapelets_light(x, y, z, z, one, amps, 5, interpolate=False)
+    assert np.allclose(a.numpy(), b.numpy(), rtol=1e-5, atol=1e-4)
+
+
+def test_shapelet_table_cut_and_slope():
+    """The table is cut to 0 past [-5, 5] (fill values of the interpolation),
+    NaN stays NaN, and the derivative is the bracket's slope."""
+    tab = O.shapelet_table(8)
+    assert tab.shape == (9, 6000) and tab.dtype == np.float32
+    t = torch.tensor([-5.5, -5.0, 5.0, 6.0, float("nan")], dtype=torch.float64)
+    v = O.interp_regular_1d(t, tab[4])
+    assert float(v[0]) == 0.0 and float(v[3]) == 0.0 and math.isnan(float(v[4]))
+    assert abs(float(v[1]) - float(tab[4][0])) < 1e-12 and abs(float(v[2]) - float(tab[4][-1])) < 1e-12
+    h = 10.0 / 5999
+    tt = torch.tensor([0.3 * h + 1.0], dtype=torch.float64, requires_grad=True)
+    (g,) = torch.autograd.grad(O.interp_regular_1d(tt, tab[7]).sum(), tt)
+    i0 = int(math.floor((1.0 + 0.3 * h + 5.0) / h))
+    assert abs(float(g) - (float(tab[7][i0 + 1]) - float(tab[7][i0])) / h) < 1e-6 * abs(float(g)) + 1e-9
