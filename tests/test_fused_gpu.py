@@ -125,6 +125,9 @@ CONFIGS = {
     "ss2_psf23": (36, 2, 23, 4),
     # planes larger than a CTA's shared memory: per-CTA slices of global memory
     "gmem_100px_ss2_psf21": (100, 2, 21, 3),
+    # the largest sub-kernel the kernels compile (side 25)
+    "max_subkernel_ss2_psf49": (24, 2, 49, 3),
+    "max_subkernel_ss1_psf25": (30, 1, 25, 3),
 }
 
 
@@ -325,3 +328,40 @@ def test_launch_config_reports_the_kernel_shape():
     big = _setup(100, 2, gaussian_psf(0.1, 0.0325, 21), 2)
     cb = big["sim"].prob_plan(big["pm"]).launch_config(3)
     assert cb["global_planes"] == 1 and cb["smem_bytes"] == 0 and cb["family"] == 4 and cb["blocks"] == 3
+
+
+def test_empty_batches_are_no_ops():
+    """bs = 0 through every entry point: success, and no output is written."""
+    s = _setup(40, 2, gaussian_psf(0.1, 0.0325, 13), 2)
+    plan = s["sim"].prob_plan(s["pm"])
+    x = torch.zeros(1, 22, device="cuda")      # never read
+    sentinel = torch.full((4,), 7.0, device="cuda")
+    for fn, args in (("gl_forward", (N.ptr(sentinel), N.ptr(sentinel), None, None)),
+                     ("gl_forward_grad", (N.ptr(sentinel), N.ptr(sentinel), N.ptr(sentinel), None)),
+                     ("gl_log_prob", (N.ptr(sentinel), N.ptr(sentinel), N.ptr(sentinel), None))):
+        N.call(fn, plan.handle, N.ptr(x), None, 0, *args, N.stream_ptr())
+    torch.cuda.synchronize()
+    assert torch.all(sentinel == 7.0)
+
+
+def test_sample_results_do_not_depend_on_batch_neighbours():
+    """A chain's log-likelihood, chi^2 and gradient are the same alone and in
+    a batch (bitwise: fixed reduction order per sample), once the batch's
+    EPL term count -- the reference's batch-coupled rule -- is the same."""
+    s = _setup(40, 2, gaussian_psf(0.1, 0.0325, 13), 6, seed=3)
+    x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
+    e = (x[:, 2] ** 2 + x[:, 3] ** 2)           # EPL e1, e2 columns of the default model
+    order = torch.argsort(e, descending=True)
+    x = x[order].contiguous()                    # row 0 holds the most elliptical lens
+    out = {}
+    for bs in (6, 2):
+        plan = s["sim"].prob_plan(s["pm"])
+        logL, chi2 = torch.empty(bs, device="cuda"), torch.empty(bs, device="cuda")
+        grad = torch.empty(bs, x.shape[1], device="cuda")
+        xb = x[:bs].contiguous()
+        N.call("gl_forward_grad", plan.handle, N.ptr(xb), None, bs, N.ptr(logL), N.ptr(chi2), N.ptr(grad), None,
+               N.stream_ptr())
+        torch.cuda.synchronize()
+        out[bs] = (logL, chi2, grad)
+    for a, b in zip(out[6], out[2]):
+        assert torch.equal(a[:2], b[:2])

@@ -59,7 +59,8 @@ def _obs(n, rng):
 
 
 @pytest.mark.parametrize("n,ss,k,n_max,ll", [(40, 2, 21, 4, False), (48, 2, 13, 8, False), (36, 1, 13, 3, True),
-                                            (44, 2, 11, 5, True), (32, 1, 11, 3, False), (120, 2, 21, 2, False)])
+                                            (44, 2, 11, 5, True), (32, 1, 11, 3, False), (120, 2, 21, 2, False),
+                                            (32, 2, 13, 9, True)])   # the most channels: 55 shapelets + 1
 def test_lstsq_simulate_matches_oracle(n, ss, k, n_max, ll):
     from gigalens_gb300.cuda.model import BackwardProbModel
     from gigalens_gb300.cuda.simulator import LensSimulator
