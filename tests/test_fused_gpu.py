@@ -365,3 +365,40 @@ def test_sample_results_do_not_depend_on_batch_neighbours():
         out[bs] = (logL, chi2, grad)
     for a, b in zip(out[6], out[2]):
         assert torch.equal(a[:2], b[:2])
+
+
+def test_rotated_anisotropic_pixel_grid():
+    """A general transform_pix2angle (rotation by 30 degrees, pixel sides
+    0.06" x 0.07"; simulator.py:91-125 grid, tf/simulator.py:19-29
+    conversion factor det(T)): image, logL and gradient against the oracle."""
+    from gigalens_gb300.cuda.model import ForwardProbModel
+    from gigalens_gb300.cuda.simulator import LensSimulator
+
+    a = math.radians(30.0)
+    R = np.array([[math.cos(a), -math.sin(a)], [math.sin(a), math.cos(a)]])
+    T = (R @ np.diag([0.06, 0.07])).astype(np.float32)
+    n, ss, bs = 40, 2, 4
+    ksub = gaussian_psf(0.1, 0.0325, 13)
+    cfg = SimulatorConfig(delta_pix=0.065, num_pix=n, supersample=ss, kernel_supersampled=ksub, transform_pix2angle=T)
+    ocfg = O.SimConfig(0.065, n, ss, ksub.astype(np.float64), transform_pix2angle=T)
+    prior = default_prior()
+    truth = prior.sample(1, seed=101)
+    im_t = O.simulate(ORACLE_MODEL, ocfg, [[{k: v.double() for k, v in d.items()} for d in g] for g in truth])
+    obs = (im_t[0].numpy() + np.random.default_rng(0).normal(scale=0.2, size=(n, n))).astype(np.float32)
+    pm = ForwardProbModel(prior, obs, background_rms=0.2, exp_time=1000.0)
+    sim = LensSimulator(default_physmodel(), cfg, bs=bs)
+    xs = prior.sample(bs, seed=2)
+    got = sim.simulate(xs).double().cpu()
+    ref = O.simulate(ORACLE_MODEL, ocfg, [[{k: v.double() for k, v in d.items()} for d in g] for g in xs])
+    _check_images(got.reshape(ref.shape), ref)
+    s = dict(omodel=ORACLE_MODEL, ocfg=ocfg, obs=obs)
+    plan = sim.prob_plan(pm)
+    x = flat_from_struct(xs).float().cuda().contiguous()
+    logL, chi2, grad = torch.empty(bs, device="cuda"), torch.empty(bs, device="cuda"), torch.empty_like(x)
+    N.call("gl_forward_grad", plan.handle, N.ptr(x), None, bs, N.ptr(logL), N.ptr(chi2), N.ptr(grad), None,
+           N.stream_ptr())
+    torch.cuda.synchronize()
+    ll, c2, g = _oracle_loglik(s, x.double().cpu())
+    _check_scalar(logL, ll, 1e-4, name="logL")
+    _check_scalar(chi2, c2, 1e-4, name="chi2")
+    _check_grad(grad, g)

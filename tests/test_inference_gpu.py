@@ -117,3 +117,27 @@ def test_distributed_flags_single_process(default_prior, default_physmodel):
     assert torch.equal(seq.best(), z[torch.argmax(lps)])
     q_z, losses = seq.SVI(Adam(1e-3), seq.best(), n_vi=8, num_steps=3, distributed=True)
     assert torch.isfinite(losses).all()
+
+
+def test_hmc_chees_and_dual_averaging_match_target_when_likelihood_is_flat(default_prior, default_physmodel):
+    """The reference's adaptive kernel (GradientBasedTrajectoryLengthAdaptation
+    + DualAveragingStepSizeAdaptation, tf/inference.py:111-125) on a flat
+    likelihood: the chains reproduce the unconstrained prior's moments."""
+    from gigalens_gb300.cuda.diagnostics import potential_scale_reduction
+    from gigalens_gb300.cuda.inference import MultivariateNormalTriL
+
+    seq, pm = _seq(default_prior, default_physmodel, data=(np.zeros((20, 20)), 1e4, 100))
+    zs = pm.bij.inverse(default_prior.sample(20000, seed=6)).double()
+    mean, cov = zs.mean(0), torch.cov(zs.T)
+    q = MultivariateNormalTriL(mean.float().cuda(), torch.linalg.cholesky(cov).float().cuda())
+    samples, stats = seq.HMC(q, init_eps=0.3, init_l=3, n_hmc=512, num_burnin_steps=100, num_results=150,
+                             max_leapfrog_steps=30, seed=5)
+    s = samples.double().cpu()
+    acc = float(stats["accept_ratio"][100:].mean())
+    assert 0.5 < acc <= 1.0
+    assert int(stats["leapfrog_steps"][-1]) >= 1
+    flat = s.reshape(-1, s.shape[-1])
+    sd = cov.diagonal().sqrt()
+    assert ((flat.mean(0) - mean).abs() / sd).max() < 0.1
+    assert ((flat.std(0) / sd) - 1).abs().max() < 0.1
+    assert potential_scale_reduction(s.float()).max() < 1.05
