@@ -532,8 +532,9 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
     delete plan;
     return rc;
   }
-  if (!plan->fused_fits && !lsq_model && plan->family != FAM_GENERIC) {
-    // planes in global memory are a general-path mode
+  if (!plan->fused_fits && !lsq_model && plan->family != FAM_GENERIC &&
+      plan->family != FAM_EPL_SHEAR_SE_SE) {
+    // planes in global memory: the headline family and the general path
     rc = resolve_generic(model, false, &plan->gen, &plan->epl, &plan->shear);
     if (rc) {
       cudaFree(plan->dev_buf);

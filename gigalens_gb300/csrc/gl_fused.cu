@@ -42,16 +42,27 @@ int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream) {
     if (g_sm_count <= 0) g_sm_count = 1;
   }
   int grid = a.bs < g_sm_count ? a.bs : g_sm_count;
-  if (a.gscratch) smem_bytes = 0;   // planes in global memory
-  switch (a.family) {
-    case FAM_EPL_SHEAR_SE_SE: fam_launch<FAM_EPL_SHEAR_SE_SE>(a, grid, smem_bytes, stream); break;
-    case FAM_EPL_SHEAR_SE: fam_launch<FAM_EPL_SHEAR_SE>(a, grid, smem_bytes, stream); break;
-    case FAM_EPL_SE_SE: fam_launch<FAM_EPL_SE_SE>(a, grid, smem_bytes, stream); break;
-    case FAM_EPL_SE: fam_launch<FAM_EPL_SE>(a, grid, smem_bytes, stream); break;
-    case FAM_GENERIC: fam_launch<FAM_GENERIC>(a, grid, smem_bytes, stream); break;
-    default:
-      set_error("unknown model family %d", a.family);
-      return GL_ERR_INVALID;
+  if (a.gscratch) {
+    // planes in global memory: the headline family and the general path
+    // have such instantiations (plan creation routes the others to the latter)
+    switch (a.family) {
+      case FAM_EPL_SHEAR_SE_SE: fam_launch<FAM_EPL_SHEAR_SE_SE, true>(a, grid, 0, stream); break;
+      case FAM_GENERIC: fam_launch<FAM_GENERIC, true>(a, grid, 0, stream); break;
+      default:
+        set_error("model family %d has no global-memory plane kernel", a.family);
+        return GL_ERR_INVALID;
+    }
+  } else {
+    switch (a.family) {
+      case FAM_EPL_SHEAR_SE_SE: fam_launch<FAM_EPL_SHEAR_SE_SE, false>(a, grid, smem_bytes, stream); break;
+      case FAM_EPL_SHEAR_SE: fam_launch<FAM_EPL_SHEAR_SE, false>(a, grid, smem_bytes, stream); break;
+      case FAM_EPL_SE_SE: fam_launch<FAM_EPL_SE_SE, false>(a, grid, smem_bytes, stream); break;
+      case FAM_EPL_SE: fam_launch<FAM_EPL_SE, false>(a, grid, smem_bytes, stream); break;
+      case FAM_GENERIC: fam_launch<FAM_GENERIC, false>(a, grid, smem_bytes, stream); break;
+      default:
+        set_error("unknown model family %d", a.family);
+        return GL_ERR_INVALID;
+    }
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

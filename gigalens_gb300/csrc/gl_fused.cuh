@@ -1047,16 +1047,16 @@ static __device__ void setup_image(const DevImage& I, float* sm) {
   for (int i = threadIdx.x; i < nk; i += kThreads) sm[I.offK + i] = __ldg(I.kern + i);
 }
 
-template <int FAM>
+template <int FAM, bool GMEM>
 __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constant__ FusedArgs a) {
   extern __shared__ float4 smem_dyn[];
-  // the image planes: dynamic shared memory, or (general path only) this
-  // CTA's slice of a global, L2-resident scratch when the image does not fit
-  // in shared memory.  The fast families address shared memory directly.
+  // the image planes: dynamic shared memory, or (GMEM) this CTA's slice of a
+  // global, L2-resident scratch when the image does not fit in shared memory.
+  // Separate instantiations, so the shared-memory kernels address shared
+  // memory directly.
   float* sm;
-  if constexpr (FAM == FAM_GENERIC)
-    sm = a.gscratch ? a.gscratch + (size_t)blockIdx.x * a.cta_floats
-                    : reinterpret_cast<float*>(smem_dyn);
+  if constexpr (GMEM)
+    sm = a.gscratch + (size_t)blockIdx.x * a.cta_floats;
   else
     sm = reinterpret_cast<float*>(smem_dyn);
   __shared__ SmemStatic st;
@@ -1197,21 +1197,21 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
 // ---------------------------------------------------------------- host entries
 // Defined here, instantiated once per family in gl_fused_fam*.cu so that the
 // families compile as separate translation units (in parallel).
-template <int FAM>
+template <int FAM, bool GMEM>
 int fam_launch(const FusedArgs& a, int grid, int smem_bytes, cudaStream_t stream) {
-  fused_kernel<FAM><<<grid, kThreads, smem_bytes, stream>>>(a);
+  fused_kernel<FAM, GMEM><<<grid, kThreads, GMEM ? 0 : smem_bytes, stream>>>(a);
   return 0;
 }
 
 template <int FAM>
 cudaError_t fam_set_smem(int smem_bytes) {
-  return cudaFuncSetAttribute(fused_kernel<FAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  return cudaFuncSetAttribute(fused_kernel<FAM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
 }
 
 template <int FAM>
 int fam_static_smem() {
   cudaFuncAttributes at;
-  if (cudaFuncGetAttributes(&at, fused_kernel<FAM>) != cudaSuccess) {
+  if (cudaFuncGetAttributes(&at, fused_kernel<FAM, false>) != cudaSuccess) {
     cudaGetLastError();
     return (int)sizeof(SmemStatic);
   }

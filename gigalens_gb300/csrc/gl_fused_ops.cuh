@@ -4,7 +4,7 @@
 #include "gl_internal.cuh"
 
 namespace gl {
-template <int FAM>
+template <int FAM, bool GMEM>
 int fam_launch(const FusedArgs& a, int grid, int smem_bytes, cudaStream_t stream);
 template <int FAM>
 cudaError_t fam_set_smem(int smem_bytes);
