@@ -471,8 +471,10 @@ def run_ours(args):
     from gigalens_gb300.cuda.simulator import LensSimulator
 
     bs = args.chains
+    n_pix, psf = args.num_pix, 2 * args.psf_base - 1
+    default_size = (n_pix, args.psf_base) == (N_PIX, PSF_BASE)
     phys = W.physical_model()
-    cfg = W.config1()
+    cfg = W.config1() if default_size else W.sim_config(n_pix, args.psf_base)
     truth_sim = LensSimulator(phys, cfg, bs=1)
     im = truth_sim.simulate(W.draw_params(1, seed=0)).cpu().numpy().astype(np.float64)
     obs = make_observed_np(im, W.EXP_TIME, W.BG_RMS)
@@ -561,7 +563,7 @@ def run_ours(args):
         t_e2e = float(tt)
     e2e_value = ws * bs / (t_e2e * 1e-3)
 
-    fwd, adj = flops_per_eval(K)
+    fwd, adj = flops_per_eval(K, n=n_pix, k=psf)
     achieved = (fwd + adj) * bs / (t_step * 1e-3) / 1e12
 
     secondary = None
@@ -577,19 +579,23 @@ def run_ours(args):
                          % (args.cpu_chains, reps, el)}
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        metric = METRIC if default_size and bs == 4096 else "lik+grad evals/s @%dx%d^2px" % (bs, n_pix)
+        lc = plan.launch_config(bs)
+        line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": "4096 chains x 90x90 px, ss=2, PSF 41x41 (supersampled Gaussian, FWHM "
+                "config": {"workload": "%d chains x %dx%d px, ss=2, PSF %dx%d (supersampled Gaussian, FWHM "
                                        "0.1\"), EPL(50)+shear, SersicEllipse lens light + source; one fused "
-                                       "forward+adjoint launch per step",
+                                       "forward+adjoint launch per step" % (bs, n_pix, n_pix, psf, psf),
                            "chains_per_gpu": bs, "epl_terms": K, "l2": "flushed between steps (256 MiB write)",
+                           "image_planes": "global memory (L2)" if lc["global_planes"] else "shared memory",
                            "wall_s_timed": t_wall, "finite": finite},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(z.numel() * 4),
                         "d2h_bytes_per_step": int(out_host.numel() * 4),
                         "api": "ForwardProbModel.log_prob + torch.autograd.grad, pinned host buffers"},
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                             "frac": achieved / fp32_peak, "traffic": args.traffic_per_launch,
+                             "frac": achieved / fp32_peak,
+                             "traffic": args.traffic_per_launch if default_size and bs == 4096 else None,
                              "flop_per_eval": fwd + adj,
                              "peak_source": "FP32 FMA probe kernel measured in this run (MEASURED_PEAKS.json "
                                             "holds no FP32 figure)"},
@@ -614,6 +620,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--chains", type=int, default=4096)
+    ap.add_argument("--num-pix", type=int, default=N_PIX, help="image side (base pixels)")
+    ap.add_argument("--psf-base", type=int, default=PSF_BASE,
+                    help="PSF side at base scale (the supersampled kernel has 2 * side - 1)")
     ap.add_argument("--cpu-chains", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-chains", type=int, default=8)
