@@ -1199,6 +1199,15 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
 // families compile as separate translation units (in parallel).
 template <int FAM, bool GMEM>
 int fam_launch(const FusedArgs& a, int grid, int smem_bytes, cudaStream_t stream) {
+  if constexpr (GMEM) {
+    // no dynamic shared memory: give the SM's unified memory to L1, which
+    // then holds the planes' working rows and the threads' local arrays
+    static const bool carveout_set = [] {
+      return cudaFuncSetAttribute(fused_kernel<FAM, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxL1) == cudaSuccess;
+    }();
+    (void)carveout_set;
+  }
   fused_kernel<FAM, GMEM><<<grid, kThreads, GMEM ? 0 : smem_bytes, stream>>>(a);
   return 0;
 }

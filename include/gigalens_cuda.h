@@ -84,9 +84,9 @@ extern "C" {
  * respect to explicit shapelet amplitudes are computed for one shapelet
  * profile per model (more give GL_ERR_UNSUPPORTED).
  * Images whose supersampled planes exceed a CTA's shared memory (about 90 x 90
- * at ss = 2 with a 41-pixel PSF) keep them in a per-CTA slice of a global
- * scratch owned by the plan: calls on one such plan must not overlap on the
- * GPU (one stream, or serialised).                                         */
+ * at ss = 2 with a 41-pixel PSF), and every image on the general path, keep
+ * them in a per-CTA slice of a global scratch owned by the plan: calls on one
+ * such plan must not overlap on the GPU (one stream, or serialised).       */
 typedef struct {
   int type;                        /* GL_PROF_*                            */
   int group;                       /* GL_GROUP_*                           */
