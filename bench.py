@@ -140,8 +140,9 @@ def make_observed_np(im_truth, exp_time, bg):
     return (counts + rng.normal(scale=bg, size=im_truth.shape)).astype(np.float32)
 
 
-def cpu_port_rate(n_chains, seconds_hint=None):
-    """Float32 PyTorch-CPU restatement (oracle) of lik+grad on n chains."""
+def cpu_port_setup(n_chains):
+    """Float32 PyTorch-CPU restatement (oracle) of lik+grad on n chains of the
+    workload: returns (one evaluation as a callable, the EPL term count)."""
     import torch
 
     from oracle import lens_oracle as O
@@ -172,6 +173,14 @@ def cpu_port_rate(n_chains, seconds_hint=None):
         return xx.grad
 
     once()
+    return once, K
+
+
+def cpu_port_time(once, n_chains, seconds_hint=None):
+    """Repeat one evaluation for about seconds_hint (at most 50 times):
+    (evals/s, threads, repetitions, seconds)."""
+    import torch
+
     t0 = time.perf_counter()
     reps = 0
     while True:
@@ -181,7 +190,13 @@ def cpu_port_rate(n_chains, seconds_hint=None):
         if seconds_hint is None or el > seconds_hint or reps >= 50:
             break
     el = time.perf_counter() - t0
-    return n_chains * reps / el, torch.get_num_threads(), reps, el, K
+    return n_chains * reps / el, torch.get_num_threads(), reps, el
+
+
+def cpu_port_rate(n_chains, seconds_hint=None):
+    once, K = cpu_port_setup(n_chains)
+    r, cores, reps, el = cpu_port_time(once, n_chains, seconds_hint)
+    return r, cores, reps, el, K
 
 
 def dist_env():
@@ -194,9 +209,12 @@ def run_reference(args):
     if rank != 0:
         return
     n = args.ref_chains
-    rates, K, cores = [], None, None
+    once, K = cpu_port_setup(n)
+    # each step a bounded sample: the whole run stays near two minutes
+    per_step = min(args.ref_seconds, max(1.0, 120.0 / (args.warmup + args.steps)))
+    rates, cores = [], None
     for i in range(args.warmup + args.steps):
-        r, cores, reps, el, K = cpu_port_rate(n, seconds_hint=args.ref_seconds)
+        r, cores, reps, el = cpu_port_time(once, n, seconds_hint=per_step)
         if i >= args.warmup:
             rates.append(r)
     val = statistics.median(rates)
