@@ -24,7 +24,6 @@ int fused_kernel_prepare(int smem_bytes) {
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SHEAR_SE>(smem_bytes);
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SE_SE>(smem_bytes);
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SE>(smem_bytes);
-  if (e == cudaSuccess) e = fam_set_smem<FAM_GENERIC>(smem_bytes);
   if (e != cudaSuccess) {
     set_error("cudaFuncSetAttribute(max dynamic smem %d): %s", smem_bytes, cudaGetErrorString(e));
     return GL_ERR_CUDA;
@@ -58,7 +57,9 @@ int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream) {
       case FAM_EPL_SHEAR_SE: fam_launch<FAM_EPL_SHEAR_SE, false>(a, grid, smem_bytes, stream); break;
       case FAM_EPL_SE_SE: fam_launch<FAM_EPL_SE_SE, false>(a, grid, smem_bytes, stream); break;
       case FAM_EPL_SE: fam_launch<FAM_EPL_SE, false>(a, grid, smem_bytes, stream); break;
-      case FAM_GENERIC: fam_launch<FAM_GENERIC, false>(a, grid, smem_bytes, stream); break;
+      case FAM_GENERIC:
+        set_error("the general path needs the plan's global plane scratch");
+        return GL_ERR_INVALID;
       default:
         set_error("unknown model family %d", a.family);
         return GL_ERR_INVALID;

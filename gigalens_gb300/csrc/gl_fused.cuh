@@ -1217,10 +1217,11 @@ cudaError_t fam_set_smem(int smem_bytes) {
   return cudaFuncSetAttribute(fused_kernel<FAM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
 }
 
+// (the general path exists only with global planes)
 template <int FAM>
 int fam_static_smem() {
   cudaFuncAttributes at;
-  if (cudaFuncGetAttributes(&at, fused_kernel<FAM, false>) != cudaSuccess) {
+  if (cudaFuncGetAttributes(&at, fused_kernel<FAM, FAM == FAM_GENERIC>) != cudaSuccess) {
     cudaGetLastError();
     return (int)sizeof(SmemStatic);
   }

@@ -1,8 +1,8 @@
-// Fused kernel, family FAM_GENERIC (one translation unit per family).
+// Fused kernel, family FAM_GENERIC (the general path), which keeps its image
+// planes in a per-CTA slice of global memory at every image size.
 #include "gl_fused.cuh"
 
 namespace gl {
-template int fam_launch<FAM_GENERIC, false>(const FusedArgs&, int, int, cudaStream_t);
-template cudaError_t fam_set_smem<FAM_GENERIC>(int);
+template int fam_launch<FAM_GENERIC, true>(const FusedArgs&, int, int, cudaStream_t);
 template int fam_static_smem<FAM_GENERIC>();
 }  // namespace gl
