@@ -403,3 +403,31 @@ def test_rotated_anisotropic_pixel_grid():
     _check_scalar(logL, ll, 1e-4, name="logL")
     _check_scalar(chi2, c2, 1e-4, name="chi2")
     _check_grad(grad, g)
+
+
+def test_gradient_matches_fp64_central_differences_on_64_samples():
+    """The 90x90 configuration's gradient check: 64 random samples, the
+    kernel's d logL / dx against float64 central differences of the oracle
+    (step 1e-6 max(1, |x|) per component), within 1e-3 relative or twice the
+    float32 noise band of the reference's own arithmetic."""
+    n, ss, bs = 90, 2, 64
+    s = _setup(n, ss, gaussian_psf(0.1, 0.0325, 41), bs, seed=11)
+    plan = s["sim"].prob_plan(s["pm"])
+    x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
+    logL, chi2, grad = torch.empty(bs, device="cuda"), torch.empty(bs, device="cuda"), torch.empty_like(x)
+    N.call("gl_forward_grad", plan.handle, N.ptr(x), None, bs, N.ptr(logL), N.ptr(chi2), N.ptr(grad), None,
+           N.stream_ptr())
+    torch.cuda.synchronize()
+    x64 = x.double().cpu()
+    obs64 = s["obs"].astype(np.float64)
+    fd = torch.zeros_like(x64)
+    for j in range(x64.shape[1]):
+        h = 1e-6 * torch.clamp(x64[:, j].abs(), min=1.0)
+        e = torch.zeros_like(x64)
+        e[:, j] = h
+        lp, _ = O.forward_log_likelihood_flat(s["omodel"], s["ocfg"], x64 + e, obs64, 0.2, 1000.0)
+        lm, _ = O.forward_log_likelihood_flat(s["omodel"], s["ocfg"], x64 - e, obs64, 0.2, 1000.0)
+        fd[:, j] = (lp - lm) / (2 * h)
+    band = fp32_band(lambda xx: O.forward_log_likelihood_flat(
+        s["omodel"], s["ocfg"], xx, s["obs"], 0.2, 1000.0, dtype=torch.float32)[0], x64.float(), fd, n_perturb=2)
+    _check_grad(grad, (fd, band), "d logL / dx vs FP64 central differences")
