@@ -416,6 +416,7 @@ static void fill_args(const gl_plan* plan, FusedArgs& a) {
   a.gen = plan->gen;
   a.gscratch = plan->gscratch;
   a.cta_floats = plan->cta_floats;
+  a.n_cta = plan->n_cta;
   a.has_prior = plan->has_prior;
   for (int i = 0; i < GL_MAX_PARAMS; ++i) a.prior[i] = plan->prior[i];
   a.img_stride = plan->max_pix;

@@ -8,8 +8,8 @@
 
 namespace gl {
 
-static int g_sm_count = 0;
-static int g_smem_set = -1;   // dynamic smem attribute already set (only ever raised)
+static int g_sm_count[kMaxDevices];   // per device, 0 until read
+static int g_smem_set[kMaxDevices];   // dynamic smem attribute set per device (only ever raised)
 
 // Largest static shared-memory footprint over the fused kernel's families.
 int fused_static_smem_bytes() {
@@ -19,7 +19,8 @@ int fused_static_smem_bytes() {
 }
 
 int fused_kernel_prepare(int smem_bytes) {
-  if (smem_bytes <= g_smem_set) return GL_OK;
+  const int dev = current_device_slot();
+  if (smem_bytes <= g_smem_set[dev]) return GL_OK;
   cudaError_t e = fam_set_smem<FAM_EPL_SHEAR_SE_SE>(smem_bytes);
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SHEAR_SE>(smem_bytes);
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SE_SE>(smem_bytes);
@@ -28,20 +29,22 @@ int fused_kernel_prepare(int smem_bytes) {
     set_error("cudaFuncSetAttribute(max dynamic smem %d): %s", smem_bytes, cudaGetErrorString(e));
     return GL_ERR_CUDA;
   }
-  g_smem_set = smem_bytes;
+  g_smem_set[dev] = smem_bytes;
   return GL_OK;
 }
 
 int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream) {
   if (a.bs <= 0) return GL_OK;
-  if (g_sm_count == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
-    if (g_sm_count <= 0) g_sm_count = 1;
+  const int dev = current_device_slot();
+  if (g_sm_count[dev] == 0) {
+    int d = 0, n = 0;
+    cudaGetDevice(&d);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d);
+    g_sm_count[dev] = n > 0 ? n : 1;
   }
-  int grid = a.bs < g_sm_count ? a.bs : g_sm_count;
+  int grid = a.bs < g_sm_count[dev] ? a.bs : g_sm_count[dev];
   if (a.gscratch) {
+    if (grid > a.n_cta) grid = a.n_cta;   // one plane slice per CTA
     // planes in global memory: the headline family and the general path
     // have such instantiations (plan creation routes the others to the latter)
     switch (a.family) {

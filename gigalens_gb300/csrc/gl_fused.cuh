@@ -1202,11 +1202,12 @@ int fam_launch(const FusedArgs& a, int grid, int smem_bytes, cudaStream_t stream
   if constexpr (GMEM) {
     // no dynamic shared memory: give the SM's unified memory to L1, which
     // then holds the planes' working rows and the threads' local arrays
-    static const bool carveout_set = [] {
-      return cudaFuncSetAttribute(fused_kernel<FAM, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                  (int)cudaSharedmemCarveoutMaxL1) == cudaSuccess;
-    }();
-    (void)carveout_set;
+    static bool carveout_set[kMaxDevices];
+    const int dev = current_device_slot();
+    if (!carveout_set[dev])
+      carveout_set[dev] = cudaFuncSetAttribute(fused_kernel<FAM, true>,
+                                               cudaFuncAttributePreferredSharedMemoryCarveout,
+                                               (int)cudaSharedmemCarveoutMaxL1) == cudaSuccess;
   }
   fused_kernel<FAM, GMEM><<<grid, kThreads, GMEM ? 0 : smem_bytes, stream>>>(a);
   return 0;

@@ -196,15 +196,16 @@ __global__ void __launch_bounds__(kGT) lsq_gram_tc_kernel(const __grid_constant_
 int gram_tc_smem_bytes() { return kGramSmem; }
 
 int launch_gram_tc(const LsqArgs& a, float* G, int* status, int grid, cudaStream_t stream) {
-  static bool attr_set = false;
-  if (!attr_set) {
+  static bool attr_set[kMaxDevices];   // per device
+  const int dev = current_device_slot();
+  if (!attr_set[dev]) {
     cudaError_t e = cudaFuncSetAttribute(lsq_gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          kGramSmem);
     if (e != cudaSuccess) {
       set_error("Gram kernel shared memory attribute: %s", cudaGetErrorString(e));
       return GL_ERR_CUDA;
     }
-    attr_set = true;
+    attr_set[dev] = true;
   }
   lsq_gram_tc_kernel<<<grid, kGT, kGramSmem, stream>>>(a, G, status);
   return GL_OK;

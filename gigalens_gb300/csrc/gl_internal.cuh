@@ -23,6 +23,7 @@ constexpr float kShpTabLo = -5.f, kShpTabHi = 5.f;
 constexpr int kGenMass = 2;          // general path: mass profiles besides SHEAR
 constexpr int kGenLight = 3;         // general path: light profiles
 constexpr int kMaxAmps = 64;         // general path: external amplitudes per sample
+constexpr int kMaxDevices = 64;      // per-device caches of launch attributes
 
 // Per-image constants, in device-ready form.
 struct DevImage {
@@ -128,6 +129,7 @@ struct FusedArgs {
   int want_grad;            // run the adjoint phases
   float* gscratch;          // images too large for shared memory: per-CTA planes in
   int cta_floats;           //   global memory (cta_floats per CTA), else null
+  int n_cta;                //   slices in gscratch: the grid never exceeds it
 };
 
 }  // namespace gl
@@ -160,6 +162,13 @@ namespace gl {
 // implemented in gl_fused.cu
 int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream);
 int fused_kernel_prepare(int smem_bytes);
+// The current device as an index into the per-device caches (ids at or
+// above kMaxDevices share the last slot).
+inline int current_device_slot() {
+  int d = 0;
+  cudaGetDevice(&d);
+  return d < 0 ? 0 : (d < kMaxDevices ? d : kMaxDevices - 1);
+}
 int fused_static_smem_bytes();
 // implemented in gl_profile_eval.cu
 int launch_profile_eval(int type, const float* x, const float* y, int64_t n, const float* params,

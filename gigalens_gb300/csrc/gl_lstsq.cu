@@ -633,7 +633,7 @@ __global__ void __launch_bounds__(256) lsq_image_kernel(const __grid_constant__ 
 }
 
 // ------------------------------------------------------------------ host side
-static int g_lsq_smem_set = -1;
+static int g_lsq_smem_set[kMaxDevices];   // basis kernel smem attribute set per device
 
 int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
   LsqPlan* L = new LsqPlan;
@@ -827,7 +827,8 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
     L->img[i].err = (const float*)base;
     base += ((size_t)errs[i].size() * 4 + 255) / 256 * 256;
   }
-  if (smem > g_lsq_smem_set) {
+  const int dev_slot = current_device_slot();
+  if (smem > g_lsq_smem_set[dev_slot]) {
     cudaError_t e = cudaFuncSetAttribute(lsq_basis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) {
       set_error("lsq smem attribute: %s", cudaGetErrorString(e));
@@ -835,7 +836,7 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
       delete L;
       return GL_ERR_CUDA;
     }
-    g_lsq_smem_set = smem;
+    g_lsq_smem_set[dev_slot] = smem;
   }
   plan->lsq = L;
   return GL_OK;
