@@ -355,7 +355,8 @@ def run_sequence(args):
                                                  n_vi=1024, num_steps=args.seq_svi_steps))
     (samples, stats), t_hmc = timed(lambda: seq.HMC(q_z, init_eps=0.3, init_l=8, n_hmc=args.seq_hmc_chains,
                                                     num_burnin_steps=500, num_results=args.seq_hmc_results,
-                                                    adapt_trajectory=False))
+                                                    adapt_trajectory=False,
+                                                    step_size_reduce=args.seq_step_reduce))
     rhat = potential_scale_reduction(samples)
     ess = effective_sample_size(samples)
     # posterior in physical space, against the truth
@@ -383,6 +384,7 @@ def run_sequence(args):
             "map_best_chi2_per_dof": map_chi2_dof,
             "svi_loss_first_last": [float(losses[0]), float(losses[-1])],
             "hmc_accept_ratio_kept": float(acc[500:].mean()), "hmc_step_size": float(stats["step_size"][-1]),
+            "hmc_step_size_reduce": args.seq_step_reduce,
             "rhat_max": float(rhat.max()), "rhat_median": float(rhat.median()),
             "ess_min": float(ess.min()), "ess_median": float(ess.median()),
             "posterior_mean_chi2_per_dof": float(c21[0]),
@@ -661,6 +663,8 @@ def main():
     ap.add_argument("--seq-svi-steps", type=int, default=1500)
     ap.add_argument("--seq-hmc-chains", type=int, default=2048)
     ap.add_argument("--seq-hmc-results", type=int, default=1000)
+    ap.add_argument("--seq-step-reduce", default="harmonic", choices=["harmonic", "mean"],
+                    help="HMC step-size adaptation over chains: the reference's harmonic mean, or the mean")
     ap.add_argument("--ttm-pairs", type=int, default=2_000_000)
     ap.add_argument("--ttm-epochs", type=int, default=20)
     ap.add_argument("--ttm-lenses", type=int, default=256)

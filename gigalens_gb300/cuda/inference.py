@@ -195,11 +195,14 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
     # ------------------------------------------------------------------ HMC
     def HMC(self, q_z, init_eps=0.3, init_l=3, n_hmc=50, num_burnin_steps=250, num_results=750,
             max_leapfrog_steps=30, seed=3, adapt_trajectory=True, adapt_step_size=True,
-            target_accept_prob=0.75, use_graph=True, distributed=False):
+            target_accept_prob=0.75, use_graph=True, distributed=False, step_size_reduce="harmonic"):
         """Returns ``(samples, sample_stats)``; samples ``(num_results, n_hmc, d)``
         in unconstrained space.  ``distributed``: each rank runs its share of
         the ``n_hmc`` chains (seed + rank) with its own adaptation and returns
-        its samples; ``distributed.gather_chains(samples, dim=1)`` joins them."""
+        its samples; ``distributed.gather_chains(samples, dim=1)`` joins them.
+        ``step_size_reduce``: how the step-size adaptation combines the chains'
+        acceptance probabilities, "harmonic" (the reference's, TFP's default)
+        or "mean" (not dominated by the least-accepting of many chains)."""
         if distributed:
             rank, _ = D.rank_world()
             lo, hi = D.shard_range(n_hmc)
@@ -221,7 +224,7 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
         g = torch.empty_like(z)
         log_prob_and_grad(plan, z, logp, chi2, g)
         n_adapt = int(num_burnin_steps * 0.8)
-        da = _DualAveraging(init_eps, target_accept_prob, dev)
+        da = _DualAveraging(init_eps, target_accept_prob, dev, reduce=step_size_reduce)
         chees = _ChEES(init_l * init_eps, max_leapfrog_steps, dev) if adapt_trajectory else None
         total = num_burnin_steps + num_results
         samples = torch.empty((num_results, n_hmc, d), dtype=torch.float32, device=dev)
@@ -363,9 +366,15 @@ class MultivariateNormalTriL:
 
 
 class _DualAveraging:
-    """Shared step size adapted toward ``target`` mean acceptance."""
+    """Shared step size adapted toward ``target`` acceptance.  ``reduce``
+    combines the chains' acceptance probabilities: "harmonic" (the
+    log-harmonic-mean-exp of TFP's DualAveragingStepSizeAdaptation default,
+    which the least-accepting chains dominate) or "mean" (their average)."""
 
-    def __init__(self, init_eps, target, dev, shrinkage=0.05, t0=10.0, kappa=0.75):
+    def __init__(self, init_eps, target, dev, shrinkage=0.05, t0=10.0, kappa=0.75, reduce="harmonic"):
+        if reduce not in ("harmonic", "mean"):
+            raise ValueError("step_size_reduce must be 'harmonic' or 'mean'")
+        self.reduce = reduce
         self.step_size = torch.tensor([float(init_eps)], device=dev)
         self.mu = math.log(10.0 * init_eps)
         self.target, self.gamma, self.t0, self.kappa = target, shrinkage, t0, kappa
@@ -376,10 +385,13 @@ class _DualAveraging:
     def update(self, log_accept):
         self.t += 1
         t = float(self.t)
-        # log-harmonic-mean-exp of the acceptance ratios over chains
         la = torch.clamp(log_accept, max=0.0)
-        red = -(torch.logsumexp(-la, 0) - math.log(la.numel()))
-        p = torch.exp(red)
+        if self.reduce == "mean":
+            p = torch.exp(la).mean()
+        else:
+            # log-harmonic-mean-exp of the acceptance ratios over chains
+            red = -(torch.logsumexp(-la, 0) - math.log(la.numel()))
+            p = torch.exp(red)
         self.err_sum += self.target - p
         log_eps = self.mu - math.sqrt(t) / self.gamma * self.err_sum / (t + self.t0)
         w = t ** (-self.kappa)
