@@ -29,3 +29,21 @@ def test_ess_iid_and_ar1():
     ess = float(effective_sample_size(y[:, :, None])[0])
     expect = n * m * (1 - phi) / (1 + phi)
     assert 0.75 * expect < ess < 1.25 * expect
+
+
+def test_dual_averaging_reductions():
+    """The step-size adaptation's reduction over chains: the log-harmonic mean
+    (TFP's default) follows the least-accepting chain, the mean does not."""
+    import math
+
+    from gigalens_gb300.cuda.inference import _DualAveraging
+
+    la = torch.full((2048,), math.log(0.99))
+    la[0] = math.log(1e-4)                       # one chain that rejects
+    steps = {}
+    for reduce in ("harmonic", "mean"):
+        da = _DualAveraging(0.3, 0.75, torch.device("cpu"), reduce=reduce)
+        for _ in range(20):
+            da.update(la)
+        steps[reduce] = float(da.step_size[0])
+    assert steps["harmonic"] < 0.3 < steps["mean"]
