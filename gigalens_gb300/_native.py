@@ -141,6 +141,7 @@ _i64 = ctypes.c_int64
 # (name, restype, argtypes) for every function the header declares
 SIGNATURES = [
     ("gl_abi_version", _i, []),
+    ("gl_struct_size", _i, [_i]),
     ("gl_last_error", ctypes.c_char_p, []),
     ("gl_device_info", _i, [ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     ("gl_plan_create", _i, [ctypes.POINTER(gl_model_desc), ctypes.POINTER(gl_image_desc), _i,

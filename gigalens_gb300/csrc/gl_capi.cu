@@ -430,6 +430,18 @@ extern "C" {
 
 int gl_abi_version(void) { return GL_ABI_VERSION; }
 
+int gl_struct_size(int which) {
+  switch (which) {
+    case 0: return (int)sizeof(gl_profile_desc);
+    case 1: return (int)sizeof(gl_model_desc);
+    case 2: return (int)sizeof(gl_image_desc);
+    case 3: return (int)sizeof(gl_prior_leaf);
+    case 4: return (int)sizeof(gl_tune_result);
+    case 5: return (int)sizeof(gl_adam_cfg);
+    default: return -1;
+  }
+}
+
 const char* gl_last_error(void) { return g_err; }
 
 int gl_device_info(int* sm_count, int* smem_optin_bytes) {

@@ -143,6 +143,10 @@ typedef struct gl_plan gl_plan;
 
 /* ---- library ---------------------------------------------------------- */
 int gl_abi_version(void);
+/* sizeof of the public structs, for bindings to check their mirrors:
+ * 0 gl_profile_desc, 1 gl_model_desc, 2 gl_image_desc, 3 gl_prior_leaf,
+ * 4 gl_tune_result, 5 gl_adam_cfg; -1 for any other index.               */
+int gl_struct_size(int which);
 const char* gl_last_error(void);
 /* Number of SMs and the opt-in shared memory per block of the current device. */
 int gl_device_info(int* sm_count, int* smem_optin_bytes);

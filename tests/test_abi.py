@@ -42,6 +42,17 @@ def test_abi_version():
     assert N.lib().gl_abi_version() == hv == N.GL_ABI_VERSION
 
 
+def test_struct_mirrors_match_the_header():
+    """The ctypes mirrors have the C structs' sizes (a field added on one side
+    only would shift every later field)."""
+    mirrors = [N.gl_profile_desc, N.gl_model_desc, N.gl_image_desc, N.gl_prior_leaf, N.gl_tune_result,
+               N.gl_adam_cfg]
+    lib = N.lib()
+    for i, m in enumerate(mirrors):
+        assert lib.gl_struct_size(i) == ctypes.sizeof(m), (m.__name__, lib.gl_struct_size(i), ctypes.sizeof(m))
+    assert lib.gl_struct_size(len(mirrors)) == -1
+
+
 def test_bad_arguments_are_rejected_without_a_device():
     lib = N.lib()
     h = ctypes.c_void_p()
