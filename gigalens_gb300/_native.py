@@ -10,13 +10,14 @@ import threading
 
 from . import _build
 
-GL_ABI_VERSION = 3   # include/gigalens_cuda.h
+GL_ABI_VERSION = 4   # include/gigalens_cuda.h
 
 GL_OK = 0
 GL_ERR_INVALID = -1
 GL_ERR_UNSUPPORTED = -2
 GL_ERR_CUDA = -3
 GL_ERR_NOMEM = -4
+GL_ERR_INTERNAL = -5
 
 GL_PROF_NONE = 0
 GL_PROF_EPL = 1
@@ -163,6 +164,8 @@ SIGNATURES = [
     ("gl_lstsq", _i, [_vp, _vp, _vp, _i, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp]),
     ("gl_lstsq_noalloc", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
     ("gl_lstsq_grad", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    ("gl_lstsq_status", _i, [_vp, _i, _vp, _vp, _vp]),
+    ("gl_test_set_wait_polls", _i, [_i]),
     ("gl_autotune", _i, [_vp, _i, _vp]),
     ("gl_nn_gemm", _i, [_i, _i, _i, _i, _i, _i, ctypes.c_float, _vp, _i, ctypes.c_longlong, _vp, _i,
                         ctypes.c_longlong, ctypes.c_float, _vp, _i, ctypes.c_longlong, _i, _i, _vp]),

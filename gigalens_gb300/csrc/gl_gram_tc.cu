@@ -46,8 +46,14 @@ __device__ __forceinline__ uint32_t elem_off(int row, int k) {
 }
 }  // namespace
 
+// Polls of the pipeline's mbarrier waits (0 = kWaitLimit).  Only the
+// failure-detection test lowers it, to make those waits run out; the drain
+// after a timeout always waits with kWaitLimit, so no MMA is in flight when
+// the TMEM is freed.
+static unsigned g_wait_polls_override = 0;
+
 __global__ void __launch_bounds__(kGT) lsq_gram_tc_kernel(const __grid_constant__ LsqArgs a, float* G,
-                                                          int* status) {
+                                                          int* status, uint32_t wait_polls) {
   extern __shared__ __align__(1024) unsigned char gsm[];
   // layout: [0, 1024) control; stages; float64 G copy
   uint64_t* mbar = reinterpret_cast<uint64_t*>(gsm);          // 2 barriers
@@ -107,7 +113,7 @@ __global__ void __launch_bounds__(kGT) lsq_gram_tc_kernel(const __grid_constant_
       unsigned char* tile_lo = tile_hi + kTileBytes;
       // the stage's previous MMAs (chunk gchunk - 2) must be done before refilling
       if (gchunk >= 2) {
-        const bool ok = mbar_wait(&mbar[s], ((gchunk - 2) >> 1) & 1u, kWaitLimit);
+        const bool ok = mbar_wait(&mbar[s], ((gchunk - 2) >> 1) & 1u, wait_polls);
         if (__syncthreads_or(!ok)) {
           failed = true;
           break;
@@ -147,7 +153,7 @@ __global__ void __launch_bounds__(kGT) lsq_gram_tc_kernel(const __grid_constant_
       ++seg_pos;
       // end of a segment (or of the sample): add the accumulator into G64
       if (seg_pos == kSegChunks || ch == nchunks - 1) {
-        const bool ok = mbar_wait(&mbar[s], (gchunk >> 1) & 1u, kWaitLimit);
+        const bool ok = mbar_wait(&mbar[s], (gchunk >> 1) & 1u, wait_polls);
         if (__syncthreads_or(!ok)) {
           failed = true;
           break;
@@ -207,8 +213,11 @@ int launch_gram_tc(const LsqArgs& a, float* G, int* status, int grid, cudaStream
     }
     attr_set[dev] = true;
   }
-  lsq_gram_tc_kernel<<<grid, kGT, kGramSmem, stream>>>(a, G, status);
+  const uint32_t polls = g_wait_polls_override ? g_wait_polls_override - 1u : kWaitLimit;
+  lsq_gram_tc_kernel<<<grid, kGT, kGramSmem, stream>>>(a, G, status, polls);
   return GL_OK;
 }
+
+void set_gram_wait_polls(int polls) { g_wait_polls_override = polls < 0 ? 0u : (unsigned)polls + 1u; }
 
 }  // namespace gl

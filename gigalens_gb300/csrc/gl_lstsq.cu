@@ -858,14 +858,16 @@ static int basis_ctas(const LsqPlan* L, int bs) {
 
 // Workspace: X [bs][D][maxP], G [bs][D][D], V [bs][D][D], h, r, ilam [bs][D],
 // beta [basis CTAs][beta_per_cta] (float2), status.
-size_t lsq_workspace_bytes(const LsqPlan* L, int bs) {
+size_t lsq_status_offset(const LsqPlan* L, int bs) {
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   const size_t X = (size_t)bs * L->D * L->maxP * 4;
   const size_t G = (size_t)bs * L->D * L->D * 4;
   const size_t h = (size_t)bs * L->D * 4;
   const size_t beta = (size_t)basis_ctas(L, bs) * L->beta_per_cta * 8;
-  return up(X) + 2 * up(G) + 3 * up(h) + up(beta) + 256;
+  return up(X) + 2 * up(G) + 3 * up(h) + up(beta);
 }
+
+size_t lsq_workspace_bytes(const LsqPlan* L, int bs) { return lsq_status_offset(L, bs) + 256; }
 
 int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, float* work,
             size_t work_bytes, float* coeffs, float* img_out, float* logL, float* chi2,
@@ -914,6 +916,10 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   a.beta_stride = L->beta_per_cta;
   base += up((size_t)n_basis * L->beta_per_cta * 8);
   int* status = (int*)base;
+  if ((size_t)((char*)status - (char*)work) != lsq_status_offset(L, bs)) {
+    set_error("least squares: workspace layout mismatch");
+    return GL_ERR_INTERNAL;
+  }
   float* co = coeffs;
   if (!co) {
     set_error("least squares: coeffs buffer required");
@@ -978,6 +984,36 @@ static int noalloc_scratch_address(int device, void** out) {
 }
 
 }  // namespace gl
+
+extern "C" int gl_lstsq_status(const gl_plan* plan, int bs, const void* work, int* status,
+                               void* stream) {
+  using namespace gl;
+  if (!plan || !plan->lsq || bs < 0 || !status) {
+    set_error("gl_lstsq_status: null plan or status, negative batch, or no least-squares profiles");
+    return GL_ERR_INVALID;
+  }
+  const char* base = (const char*)work;
+  if (!base) {
+    int dev = -1;
+    cudaGetDevice(&dev);
+    void* p = nullptr;
+    int rc = noalloc_scratch_address(dev, &p);
+    if (rc) return rc;
+    base = (const char*)p;
+  }
+  const size_t off = lsq_status_offset((const LsqPlan*)plan->lsq, bs);
+  cudaError_t e = cudaMemcpyAsync(status, base + off, sizeof(int), cudaMemcpyDefault, (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    set_error("gl_lstsq_status: %s", cudaGetErrorString(e));
+    return GL_ERR_CUDA;
+  }
+  return GL_OK;
+}
+
+extern "C" int gl_test_set_wait_polls(int polls) {
+  gl::set_gram_wait_polls(polls);
+  return GL_OK;
+}
 
 extern "C" int gl_lstsq_noalloc(const gl_plan* plan, const float* x, const int* img_id, int bs,
                                 float* coeffs, float* img_out, float* logL, float* chi2,

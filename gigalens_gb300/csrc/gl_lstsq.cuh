@@ -74,6 +74,8 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs);
 // tensor-core Gram (gl_gram_tc.cu)
 int launch_gram_tc(const LsqArgs& a, float* G, int* status, int grid, cudaStream_t stream);
 int gram_tc_smem_bytes();
+void set_gram_wait_polls(int polls);   // < 0: the default limit
+size_t lsq_status_offset(const LsqPlan* L, int bs);
 void lsq_destroy(gl_plan* plan);
 size_t lsq_workspace_bytes(const LsqPlan* L, int bs);
 int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, float* work,

@@ -76,13 +76,21 @@ def global_best(z: torch.Tensor, logp: torch.Tensor) -> torch.Tensor:
     receives it."""
     import torch.distributed as dist
 
-    lp = torch.nan_to_num(logp.detach(), nan=-float("inf"))
-    i = int(torch.argmax(lp))
-    best = z[i].detach().clone()
+    lp = torch.nan_to_num(logp.detach().reshape(-1), nan=-float("inf"))
     _, world = rank_world()
-    if world == 1:
-        return best
-    val = lp[i].reshape(1).clone()
+    if lp.numel() == 0:
+        # an empty shard (fewer chains than ranks) still takes part in the
+        # exchange, with -inf so that it never wins
+        if world == 1:
+            raise ValueError("global_best: no chains")
+        best = z.new_zeros(z.shape[1:])
+        val = torch.full((1,), -float("inf"), dtype=lp.dtype, device=lp.device)
+    else:
+        i = int(torch.argmax(lp))
+        best = z[i].detach().clone()
+        if world == 1:
+            return best
+        val = lp[i].reshape(1).clone()
     vals = [torch.empty_like(val) for _ in range(world)]
     dist.all_gather(vals, val)
     winner = int(torch.argmax(torch.cat(vals)))

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GL_ABI_VERSION 3
+#define GL_ABI_VERSION 4
 
 /* ---- error codes ---------------------------------------------------- */
 #define GL_OK 0
@@ -40,6 +40,7 @@ extern "C" {
 #define GL_ERR_UNSUPPORTED (-2)  /* valid input this build does not cover   */
 #define GL_ERR_CUDA (-3)         /* a CUDA runtime call failed              */
 #define GL_ERR_NOMEM (-4)        /* device allocation failed                */
+#define GL_ERR_INTERNAL (-5)     /* an internal consistency check failed    */
 
 /* ---- profile types (reference class names in comments) --------------- */
 #define GL_PROF_NONE 0
@@ -251,6 +252,21 @@ int gl_lstsq(const gl_plan* plan, const float* x, const int* img_id, int bs, voi
  *    threads) race on the array: serialise them.                          */
 int gl_lstsq_noalloc(const gl_plan* plan, const float* x, const int* img_id, int bs,
                      float* coeffs, float* img_out, float* logL, float* chi2, void* stream);
+
+/* Status word of the last gl_lstsq / gl_lstsq_noalloc call of bs chains on
+ * this plan (no reference counterpart: TF raises no error for this).  The
+ * Gram kernel's waits on the tensor cores are bounded; a wait that runs out
+ * sets the word to 1, the kernel drains its MMAs, frees its tensor memory and
+ * returns, and the solve writes NaN coefficients.  work: the workspace given
+ * to gl_lstsq, or NULL for gl_lstsq_noalloc's fixed scratch.  *status
+ * (device or host memory) receives the word, stream-ordered: 0 = ok.       */
+int gl_lstsq_status(const gl_plan* plan, int bs, const void* work, int* status, void* stream);
+
+/* Failure-detection test hook (no reference counterpart): the number of
+ * polls of the Gram kernel's pipeline waits for the following launches;
+ * polls < 0 restores the default limit.  0 makes every such wait run out at
+ * once.  Not for production use.                                          */
+int gl_test_set_wait_polls(int polls);
 
 /* Launch configuration of the fused kernel for a batch of bs samples.  The
  * correlation tile (16 outputs per lane, quarter-warp groups of 4 rows x 2

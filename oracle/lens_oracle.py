@@ -417,12 +417,22 @@ def _psf_pool(img, cfg: SimConfig, dtype):
     return img
 
 
-def simulate(model, cfg: SimConfig, params, dtype=torch.float64, no_deflection=False):
-    """``LensSimulator.simulate``, ``tf/simulator.py:65-97``.  Returns (bs, N, N)."""
+def simulate(model, cfg: SimConfig, params, dtype=torch.float64, no_deflection=False, ray_dtype=None):
+    """``LensSimulator.simulate``, ``tf/simulator.py:65-97``.  Returns (bs, N, N).
+
+    ``ray_dtype``: precision of the ray shooting alone (``tf/simulator.py:57-63``),
+    the rest in ``dtype``; float32 here with float64 elsewhere isolates the
+    image error that float32 deflections cause (the lensed source's profile
+    amplifies the deflection's rounding)."""
     lens_p, ll_p, src_p = _split(model, params)
     x = torch.as_tensor(cfg.img_x, dtype=dtype)[None]
     y = torch.as_tensor(cfg.img_y, dtype=dtype)[None]
-    bx, by = beta(model, lens_p, x, y, dtype)
+    if ray_dtype is None or ray_dtype == dtype:
+        bx, by = beta(model, lens_p, x, y, dtype)
+    else:
+        lp = [{k: torch.as_tensor(v).to(ray_dtype) for k, v in p.items()} for p in lens_p]
+        bx, by = beta(model, lp, x.to(ray_dtype), y.to(ray_dtype), ray_dtype)
+        bx, by = bx.to(dtype), by.to(dtype)
     if no_deflection:
         bx, by = x, y
     img = 0

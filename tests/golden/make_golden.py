@@ -1,9 +1,11 @@
 """Copy the reference's data fixtures used as golden inputs.
 
-Run in a container where the reference is mounted; writes psf.npy (the
-TinyTim F140W PSF, 13x13) and demo.npy (the 60x60 observed image of the demo
-lens) from ``src/gigalens/assets/`` of GIGA-Lens, and prints their sha256.
-The demo's true parameters are in tests/helpers.py (``demo_truth``).
+    python tests/golden/make_golden.py <GIGA-Lens checkout>/src/gigalens/assets
+
+Writes psf.npy (the TinyTim F140W PSF, 13x13) and demo.npy (the 60x60
+observed image of the demo lens) from ``src/gigalens/assets/`` of GIGA-Lens,
+and prints their sha256.  The demo's true parameters are in
+tests/helpers.py (``demo_truth``).
 """
 import hashlib
 import os
@@ -11,7 +13,9 @@ import sys
 
 import numpy as np
 
-SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src/gigalens/assets"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py <path to GIGA-Lens src/gigalens/assets>")
+SRC = sys.argv[1]
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 for name in ("psf.npy", "demo.npy"):

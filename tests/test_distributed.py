@@ -40,6 +40,13 @@ def _worker(rank, world, port, q):
         z = torch.tensor([[rank * 10.0 + 1, 0.0], [rank * 10.0 + 2, 0.0]])
         logp = torch.tensor([float(rank), float("nan")]) if rank == 0 else torch.tensor([-1.0, 5.0])
         out["best"] = D.global_best(z, logp).tolist()
+        # one chain over two ranks: rank 1's shard is empty and must not
+        # raise or leave rank 0 waiting in the exchange
+        lo1, hi1 = D.shard_range(1)
+        z1 = torch.tensor([[7.0, 8.0]])[lo1:hi1]
+        lp1 = torch.tensor([3.0])[lo1:hi1]
+        out["shard1"] = (lo1, hi1)
+        out["best1"] = D.global_best(z1, lp1).tolist()
         q.put((rank, out))
     finally:
         dist.destroy_process_group()
@@ -63,6 +70,8 @@ def test_two_rank_helpers():
         assert res[r]["gather"] == [float(i) for i in range(13)]
         assert res[r]["gather1"] == [2, 13, 3]
         assert res[r]["best"] == [12.0, 0.0]
+        assert res[r]["best1"] == [7.0, 8.0]
+    assert res[0]["shard1"] == (0, 1) and res[1]["shard1"] == (1, 1)
 
 
 def test_single_process_is_identity():
