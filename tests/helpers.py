@@ -73,3 +73,56 @@ def load_golden(name):
 
 def flat_from_struct(struct):
     return torch.stack([torch.as_tensor(v).reshape(-1) for v in tfd.flatten(struct)], dim=1)
+
+
+def image_band(omodel, ocfg, xflat, n_pert=8, seed=1):
+    """Float32 noise band of simulated images, per pixel: the largest
+    |image - float64 image| over the oracle with float32 ray shooting (the
+    rest in float64) at the input and at ``n_pert`` 1-ulp perturbations of
+    the lens parameters.  Near a steep lensed source cusp, float32
+    deflections alone move a pixel by up to ~1e-4 of its value; the reference
+    computes in float32 and carries the same noise."""
+    from oracle import lens_oracle as O
+
+    x32 = torch.as_tensor(xflat).float()
+    x64 = x32.double()
+    lens_cols = [i for i, (g, _, _) in enumerate(O.flat_layout(omodel)) if g == 0]
+    ref = O.simulate(omodel, ocfg, O.unflatten(omodel, x64))
+    r = np.random.default_rng(seed)
+    band = torch.zeros_like(ref)
+    for i in range(n_pert + 1):
+        xq = x64.clone()
+        if i:
+            pert = torch.tensor(r.choice([-1.0, 0.0, 1.0], size=(x32.shape[0], len(lens_cols))) * 2.0 ** -23,
+                                dtype=torch.float32)
+            xq[:, lens_cols] = (x32[:, lens_cols] * (1 + pert)).double()
+        im = O.simulate(omodel, ocfg, O.unflatten(omodel, xq), ray_dtype=torch.float32)
+        band = torch.maximum(band, (im - ref).abs())
+    return band
+
+
+def check_images(got, ref, band, name="image", fraction=1e-3, band_fraction=1e-3, max_rel=2e-4):
+    """Per-pixel bar on pixels above ``fraction`` of their image's maximum,
+    no absolute term: |got - ref| <= 1e-5 |ref|, or <= 1e-5 |ref| + 2 band
+    on at most ``band_fraction`` of them (``band``: ``image_band``), with a
+    relative error of at most ``max_rel`` there.  Fainter pixels:
+    |got - ref| <= 1e-6 of the image's maximum.  Prints the figures."""
+    got = got.double().cpu().reshape(ref.shape)
+    m = ref.abs().amax(dim=(-2, -1), keepdim=True)
+    sel = ref.abs() > fraction * m
+    err = (got - ref).abs()
+    lit = err <= 1e-5 * ref.abs()
+    ok = err <= 1e-5 * ref.abs() + 2.0 * band
+    need = sel & ~lit
+    rel = err / ref.abs()
+    faint = float((err / m)[~sel].max()) if bool((~sel).any()) else 0.0
+    print("\n[%s] %d pixels above %.0e of max: max rel %.2e; %d (%.3f %%) need the float32 band (max rel %.2e); "
+          "fainter pixels: max |err|/max %.2e" % (
+              name, int(sel.sum()), fraction, float(rel[sel].max()), int(need.sum()),
+              100.0 * float(need.sum()) / max(int(sel.sum()), 1), float(rel[need].max()) if bool(need.any()) else 0.0,
+              faint))
+    assert bool(ok[sel].all()), "%s: pixels outside 1e-5 + 2 band" % name
+    assert float(need.sum()) <= max(band_fraction * float(sel.sum()), 2.0), "%s: %d pixels need the band" % (
+        name, int(need.sum()))
+    assert float(rel[sel].max()) <= max_rel, name
+    assert faint <= 1e-6, name

@@ -1,18 +1,22 @@
 """Parity of the fused CUDA path with the float64 oracle.
 
 Tolerances (spec bar, per quantity, against the float64 restatement):
-  images       |d| <= 1e-5 |ref| + 1e-5 max|ref|   (per pixel; the absolute
-               floor covers the faint tail, where float32 exp/pow of the
-               reference itself loses relative accuracy)
-  logL, logp   |d| <= 1e-4 |ref|  (plus 1e-3 absolute for |ref| < 10)
+  images       pixels above 1e-3 of their image's maximum, no absolute
+               term: |d| <= 1e-5 |ref|, or 1e-5 |ref| + 2 band on at most
+               0.1 % of them (band = float32 ray-shooting noise of the
+               reference's own arithmetic, ``helpers.image_band``), relative
+               error at most 2e-4 there; fainter pixels |d| <= 1e-6 max|ref|
+               (``helpers.check_images``, which prints the figures)
+  logL, logp   |d| <= 1e-4 |ref|
   chi^2        |d| <= 1e-4 |ref|
   gradients    per component, either |d| <= 1e-3 max(|ref|, 1e-2 rms_batch(ref))
                or |d| <= 2 band, where band = max |g32 - ref| over the float32
                evaluation of the same restatement (the reference's own
                precision) at the input and at four 1-ulp perturbations of it.
                Components dominated by Sersic cusps (n > 1: the coordinate
-               derivative diverges as R^(1/n - 1)) are float32-noise-limited;
-               there the bar is "inside the reference's own float32 noise band".
+               derivative diverges as R^(1/n - 1)) are float32-noise-limited.
+               At most 2 % of the components may use the band, with a
+               relative error of at most 1e-2; both are printed.
 """
 import math
 
@@ -25,8 +29,8 @@ from gigalens_gb300 import distributions as tfd
 from gigalens_gb300.model import PhysicalModel
 from gigalens_gb300.simulator import SimulatorConfig
 from oracle import lens_oracle as O
-from tests.helpers import (ORACLE_MODEL, as_batch, default_physmodel, default_prior, demo_truth,
-                           flat_from_struct, gaussian_psf, load_golden)
+from tests.helpers import (ORACLE_MODEL, as_batch, check_images, default_physmodel, default_prior, demo_truth,
+                           flat_from_struct, gaussian_psf, image_band, load_golden)
 
 pytestmark = pytest.mark.gpu
 
@@ -82,20 +86,15 @@ def fp32_band(fn, x32, g64, n_perturb=4, seed=0):
     return worst
 
 
-def _check_images(got, ref):
-    got = got.double().cpu()
-    m = ref.abs().amax(dim=(-2, -1), keepdim=True)
-    err = (got - ref).abs()
-    tol = 1e-5 * ref.abs() + 1e-5 * m
-    worst = float((err / (1e-5 * ref.abs() + 1e-5 * m)).max())
-    assert bool((err <= tol).all()), "image mismatch: worst err/tol = %.3g, max rel-to-max %.3g" % (
-        worst, float((err / m).max()))
+def _check_images(got, ref, omodel, ocfg, xflat, name="image", **limits):
+    check_images(got, ref, image_band(omodel, ocfg, xflat), name, **limits)
 
 
-def _check_scalar(got, ref, rtol, atol_small=1e-3, name=""):
+def _check_scalar(got, ref, rtol, name=""):
     got = got.double().cpu()
-    ok = (got - ref).abs() <= rtol * ref.abs() + atol_small * (ref.abs() < 10).double()
-    assert bool(ok.all()), "%s mismatch: max rel %.3g" % (name, float(((got - ref).abs() / ref.abs()).max()))
+    rel = (got - ref).abs() / ref.abs()
+    print("\n[%s] max rel %.2e" % (name, float(rel.max())))
+    assert bool(((got - ref).abs() <= rtol * ref.abs()).all()), "%s mismatch: max rel %.3g" % (name, float(rel.max()))
 
 
 def _check_grad(got, ref, name="grad"):
@@ -104,14 +103,19 @@ def _check_grad(got, ref, name="grad"):
     floor = 1e-2 * ref.pow(2).mean(dim=0, keepdim=True).sqrt()
     scale = torch.maximum(ref.abs(), floor)
     err = (got - ref).abs()
-    ok = err <= 1e-3 * scale
-    if band is not None:
-        ok = ok | (err <= 2.0 * band)
+    lit = err <= 1e-3 * scale
+    ok = lit if band is None else lit | (err <= 2.0 * band)
     rel = err / scale
+    need = ~lit
+    print("\n[%s] %d components: max rel %.2e; %d (%.2f %%) use the float32 band, max rel among them %.2e" % (
+        name, rel.numel(), float(rel.max()), int(need.sum()), 100.0 * float(need.sum()) / rel.numel(),
+        float(rel[need].max()) if bool(need.any()) else 0.0))
     bad = (~ok).nonzero()
     assert bool(ok.all()), "%s mismatch at %s: rel %.3g (float32 band rel %s)" % (
         name, tuple(bad[0].tolist()), float(rel[tuple(bad[0].tolist())]),
         "n/a" if band is None else "%.3g" % float((band / scale)[tuple(bad[0].tolist())]))
+    assert float(need.sum()) <= max(0.02 * rel.numel(), 1.0), "%s: %d components use the band" % (name, int(need.sum()))
+    assert float(rel.max()) <= 1e-2, name
 
 
 CONFIGS = {
@@ -139,7 +143,7 @@ def test_simulate_matches_oracle(name):
     img = s["sim"].simulate(s["x_struct"])
     ref = O.simulate(ORACLE_MODEL, s["ocfg"], [[{kk: v.double() for kk, v in d.items()} for d in g]
                                                for g in s["x_struct"]])
-    _check_images(img.reshape(ref.shape), ref)
+    _check_images(img.reshape(ref.shape), ref, ORACLE_MODEL, s["ocfg"], flat_from_struct(s["x_struct"]), name)
 
 
 @pytest.mark.parametrize("name", list(CONFIGS))
@@ -391,7 +395,7 @@ def test_rotated_anisotropic_pixel_grid():
     xs = prior.sample(bs, seed=2)
     got = sim.simulate(xs).double().cpu()
     ref = O.simulate(ORACLE_MODEL, ocfg, [[{k: v.double() for k, v in d.items()} for d in g] for g in xs])
-    _check_images(got.reshape(ref.shape), ref)
+    _check_images(got.reshape(ref.shape), ref, ORACLE_MODEL, ocfg, flat_from_struct(xs), "rotated grid")
     s = dict(omodel=ORACLE_MODEL, ocfg=ocfg, obs=obs)
     plan = sim.prob_plan(pm)
     x = flat_from_struct(xs).float().cuda().contiguous()

@@ -128,6 +128,19 @@ def _setup(name, num_pix=40, ss=2, k=13, bs=6, seed=0):
                 x_struct=prior.sample(bs, seed=seed))
 
 
+# Models whose images are worse conditioned in float32 than the EPL + Sersic
+# family, so that more pixels sit inside the float32 band (all of them must):
+#  - TNFW sums terms of order tau^2 that cancel to O(x^2 ln x) near its centre
+#    (tf/profiles/mass/tnfw.py:14-38); the reference's float32 formula is off
+#    by percents there, and every ray through the centre inherits it;
+#  - explicit shapelet amplitudes make signed sums, so pixels near a zero of
+#    the image have large relative errors at any precision.
+IMAGE_LIMITS = {
+    "epl_tnfw_shear_se": dict(band_fraction=1e-2, max_rel=2e-3),
+    "sis_shapelets_explicit": dict(band_fraction=1e-2, max_rel=5e-4),
+    "sis_shapelets_interp": dict(band_fraction=1e-2, max_rel=5e-4),
+}
+
 GRAD_CASES = ["sie_shear_coresersic_se", "epl_tnfw_shear_se", "sis_se_two_sources", "sis_shapelets_explicit",
               "sis_shapelets_interp"]
 
@@ -138,7 +151,8 @@ def test_general_path_simulate(name):
     img = s["sim"].simulate(s["x_struct"])
     ref = O.simulate(s["om"], s["ocfg"], [[{k: v.double() for k, v in d.items()} for d in g]
                                           for g in s["x_struct"]])
-    _check_images(img.reshape(ref.shape), ref)
+    _check_images(img.reshape(ref.shape), ref, s["om"], s["ocfg"], flat_from_struct(s["x_struct"]), name,
+                  **IMAGE_LIMITS.get(name, {}))
 
 
 @pytest.mark.parametrize("name", GRAD_CASES)

@@ -1,8 +1,8 @@
 """Least-squares path (``lstsq_simulate``, BackwardProbModel) against the
-float64 oracle.  Images are compared relative to their maximum: the solved
-amplitudes of nearly degenerate shapelet stacks are ill-conditioned (as in
-the reference, whose float32 pinv has the same conditioning), the fitted
-image is not."""
+float64 oracle.  Images are compared relative to their maximum (bar 1e-5):
+the solved amplitudes of nearly degenerate shapelet stacks are
+ill-conditioned (as in the reference, whose float32 pinv has the same
+conditioning), the fitted image is not.  logp and chi^2: 1e-4 relative."""
 import math
 
 import numpy as np
@@ -81,14 +81,17 @@ def test_lstsq_simulate_matches_oracle(n, ss, k, n_max, ll):
     got = img.double().cpu().reshape(ref.shape)
     scale = ref.abs().amax(dim=(-2, -1), keepdim=True)
     rel = ((got - ref).abs() / scale).max()
-    assert float(rel) < 2e-4, float(rel)
     # BackwardProbModel likelihood and chi^2
     z = pm.bij.inverse(xs).float().cuda()
     logp, chi2 = pm.log_prob(sim, z)
     ll_ref, chi2_ref = O.backward_log_likelihood(ref, obs.astype(np.float64), pm.err_numpy.astype(np.float64))
     lp_ref = ll_ref + prior.log_prob(ox) + pm.unconstraining_bij.forward_log_det_jacobian(ox)
-    assert torch.allclose(logp.double().cpu(), lp_ref, rtol=1e-4, atol=1e-2)
-    assert torch.allclose(chi2.double().cpu(), chi2_ref, rtol=1e-3)
+    rlp = float(((logp.double().cpu() - lp_ref).abs() / lp_ref.abs()).max())
+    rc2 = float(((chi2.double().cpu() - chi2_ref).abs() / chi2_ref.abs()).max())
+    print("\n[lstsq %d px n_max %d] image max |err|/max %.2e, logp max rel %.2e, chi2 max rel %.2e"
+          % (n, n_max, float(rel), rlp, rc2))
+    assert float(rel) <= 1e-5
+    assert rlp <= 1e-4 and rc2 <= 1e-4
 
 
 def test_lstsq_uneven_batch_two_images():
@@ -189,7 +192,9 @@ def test_lstsq_interpolated_shapelets_match_oracle():
     ref = O.lstsq_simulate(omodel, ocfg, ox, obs.astype(np.float64), pm.err_numpy.astype(np.float64))
     got = img.double().cpu().reshape(ref.shape)
     scale = ref.abs().amax(dim=(-2, -1), keepdim=True)
-    assert float(((got - ref).abs() / scale).max()) < 2e-4
+    rel = float(((got - ref).abs() / scale).max())
+    print("\n[lstsq interpolated shapelets] image max |err|/max %.2e" % rel)
+    assert rel <= 1e-5
     # the cut matters at these scales: the exact basis gives another fit
     ox_exact = dict(omodel, source_light=[("SHAPELETS", {"n_max": n_max})])
     ref_exact = O.lstsq_simulate(ox_exact, ocfg, ox, obs.astype(np.float64), pm.err_numpy.astype(np.float64))

@@ -220,3 +220,36 @@ def test_shapelet_table_cut_and_slope():
     (g,) = torch.autograd.grad(O.interp_regular_1d(tt, tab[7]).sum(), tt)
     i0 = int(math.floor((1.0 + 0.3 * h + 5.0) / h))
     assert abs(float(g) - (float(tab[7][i0 + 1]) - float(tab[7][i0])) / h) < 1e-6 * abs(float(g)) + 1e-9
+
+
+@pytest.mark.parametrize("ss", [2, 3, 4])
+def test_supersampled_psf_rebins_to_the_input(ss):
+    """supersample_kernel (the published behaviour of lenstronomy's
+    subgrid_kernel, tf/simulator.py:48-50): re-binning the fine kernel to the
+    base grid reproduces the input PSF (the reference demo's TinyTim PSF) to
+    float32 precision; odd side, unit sum."""
+    from gigalens_gb300.simulator import rebin_kernel, supersample_kernel
+
+    psf = load_golden("psf.npy").astype(np.float64)
+    psf = psf / psf.sum()
+    fine = supersample_kernel(psf, ss)
+    n = ss * psf.shape[0]
+    assert fine.dtype == np.float32 and fine.shape == ((n - 1, n - 1) if n % 2 == 0 else (n, n))
+    assert abs(float(fine.astype(np.float64).sum()) - 1.0) < 1e-6
+    back = rebin_kernel(fine, ss)
+    assert float(np.abs(back - psf).max()) <= 1e-7 * float(psf.max())
+
+
+def test_supersampled_psf_demo_chi2():
+    """The demo at ss = 2 with the base-scale PSF (kernel=psf.npy, as the
+    reference demo passes it): chi^2 at the notebook's truth stays ~1
+    (0.981 with the iterative supersampling; 0.998 with the plain spline it
+    replaced; 0.999 at ss = 1)."""
+    from gigalens_gb300.simulator import supersample_kernel
+
+    psf = load_golden("psf.npy")
+    obs = load_golden("demo.npy")
+    cfg = O.SimConfig(0.065, 60, 2, supersample_kernel(psf, 2).astype(np.float64))
+    im = O.simulate(ORACLE_MODEL, cfg, as_batch(demo_truth()))
+    _, chi2 = O.log_likelihood(im, obs, 0.2, 100)
+    assert abs(float(chi2[0]) - 0.9813) < 2e-3
