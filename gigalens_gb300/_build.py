@@ -54,8 +54,15 @@ def build(force=False, verbose=False, ptxas_info=False):
     nvcc = _nvcc()
     extra = ["-Xptxas", "-v"] if ptxas_info else []
 
+    headers = [d for d in _deps() if not d.endswith(".cu")]
+    newest_header = max((os.path.getmtime(h) for h in headers), default=0.0)
+
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        # unforced builds reuse an object newer than its source and every header
+        if (not force and not extra and os.path.exists(obj)
+                and os.path.getmtime(obj) >= max(os.path.getmtime(src), newest_header)):
+            return obj
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

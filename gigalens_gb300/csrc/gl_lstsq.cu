@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "gl_corr.cuh"
+#include "gl_cpasync.cuh"
 #include "gl_internal.cuh"
 #include "gl_profiles.cuh"
 #include "gl_profiles_gen.cuh"
@@ -357,8 +358,10 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
                                                         float* __restrict__ coeffs, int max_sweeps,
                                                         float* __restrict__ Vout, float* __restrict__ ilam,
                                                         const int* __restrict__ status) {
-  __shared__ float A[kMaxLsqChannels + 1][kMaxLsqChannels + 1];
-  __shared__ float V[kMaxLsqChannels + 1][kMaxLsqChannels + 1];
+  // rows padded to an odd number of floats: column accesses stay conflict-free
+  constexpr int kLd = (kMaxLsqChannels + 1) | 1;
+  __shared__ float A[kMaxLsqChannels + 1][kLd];
+  __shared__ float V[kMaxLsqChannels + 1][kLd];
   __shared__ float cs[kMaxLsqChannels / 2 + 1][2];
   __shared__ int pr[kMaxLsqChannels / 2 + 1][2];
   __shared__ float hs[kMaxLsqChannels + 1];
@@ -373,6 +376,7 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
     }
     for (int t = threadIdx.x; t < n; t += blockDim.x) hs[t] = (t < D) ? h[(size_t)b * D + t] : 0.f;
     __syncthreads();
+    float prev_off = INFINITY;
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
       // convergence test: off-diagonal vs diagonal Frobenius norm (block reduction)
       {
@@ -399,7 +403,15 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
         }
         __syncthreads();
       }
-      const bool done = !(red[0] > 1e-13f * red[1]);
+      // Converged when the off-diagonal part is below 1e-11 of the diagonal
+      // (|off|_F < 3.2e-6 |diag|_F), or once a sweep near the float32 floor
+      // (< 1e-8) no longer halves it: rounding alone leaves off-diagonal
+      // entries of order eps |lambda|, whose sum over D^2 entries can stay
+      // near 1e-12 for good.  NaN stops at once.
+      const float off_now = red[0], dg_now = red[1];
+      const bool done = !(off_now > 1e-11f * dg_now) ||
+                        (off_now < 1e-8f * dg_now && off_now > 0.5f * prev_off);
+      prev_off = off_now;
       __syncthreads();
       if (done) break;
       for (int round = 0; round < n - 1; ++round) {
@@ -490,76 +502,169 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
   }
 }
 
-// img = sum_c coeffs_c X_c; BackwardProbModel likelihood with the data error map.
-// Projected residual of the weighted least-squares problem, from the basis
-// itself (not from G), in one pass over X.  One block per sample; per chunk
-// of 256 pixels: (1) thread t forms e_p = W_p^2 (y_p - sum_c X_cp c_c) of
-// pixel p = chunk + t (the channel sum in float32 groups of 8 added in
-// float64) into shared memory; (2) warp w projects the chunk onto channels
-// w, w + 8, ...: r_c += sum_p X_cp e_p, lanes over pixels (coalesced, the
-// chunk's X is still in L1), float32 over a chunk's 8 pixels per lane and
-// float64 across chunks and lanes.  c = NULL gives e = W^2 y and r = h = A^T b.
-constexpr int kResidThreads = 256;
-constexpr int kResidChPerWarp = kMaxLsqChannels / (kResidThreads / 32);
-__global__ void __launch_bounds__(kResidThreads) lsq_resid_kernel(const __grid_constant__ LsqArgs a,
-                                                                  const float* __restrict__ coeffs,
-                                                                  float* __restrict__ r) {
+// Passes over the basis stack X after the normal equations, streamed from HBM
+// through a shared-memory ring (cp.async, kXRing chunks of kXT pixels x D
+// channels; one block per sample, persistent over the batch, the copies of
+// the next chunks crossing into the next sample).  Per chunk:
+//
+//  RESID  projected residual of the weighted least-squares problem from the
+//         basis itself (not from G): (1) thread t forms
+//         e_p = W_p^2 (y_p - sum_c X_cp c_c) of pixel p = chunk + t, the
+//         channel sum in float32 groups of 8 combined in float-float
+//         (TwoSum); (2) warp w projects the chunk onto channels w, w + 8, ...:
+//         r_c += sum_p X_cp e_p, lanes over pixels, float32 over a lane's 8
+//         pixels and float-float across chunks, float64 only in the final
+//         reduction over lanes.
+//  IMAGE  img = sum_c coeffs_c X_c (no conversion factor, as the reference),
+//         the Gaussian log-likelihood with the data error map and chi^2
+//         (BackwardProbModel, tf/model.py:157-163).
+constexpr int kXT = 256;      // threads = pixels per chunk
+constexpr int kXRing = 3;     // chunks in the ring
+constexpr int kXChPerWarp = (kMaxLsqChannels + (kXT / 32) - 1) / (kXT / 32);
+
+size_t xpass_smem_bytes(int D) { return (size_t)kXRing * D * kXT * 4; }
+
+template <bool IMAGE>
+__global__ void __launch_bounds__(kXT, 1) lsq_xpass_kernel(const __grid_constant__ LsqArgs a,
+                                                          const float* __restrict__ coeffs,
+                                                          float* __restrict__ r_out, float* img_out,
+                                                          float* logL, float* chi2) {
+  extern __shared__ float4 xring4[];
+  float* ring = reinterpret_cast<float*>(xring4);
   __shared__ float cf[kMaxLsqChannels];
-  __shared__ float e_s[kResidThreads];
+  __shared__ float e_s[kXT];
+  __shared__ float red[2][kXT / 32];
   const int D = a.D;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int b = blockIdx.x; b < a.bs; b += gridDim.x) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int items = D * (kXT / 4);   // 16-byte pieces of a chunk
+
+  auto valid_sample = [&](int b) {
     const int im = a.img_id ? a.img_id[b] : 0;
-    if (im < 0 || im >= a.n_images) continue;
-    const LsqImage& I = a.img[im];
+    return im >= 0 && im < a.n_images;
+  };
+  auto next_sample = [&](int b) {
+    for (b += gridDim.x; b < a.bs && !valid_sample(b); b += gridDim.x) {
+    }
+    return b;
+  };
+  int first = blockIdx.x;
+  while (first < a.bs && !valid_sample(first)) first += gridDim.x;
+  int pb = first, pch = 0;
+  auto issue = [&](int slot) {
+    if (pb < a.bs) {
+      const LsqImage& I = a.img[a.img_id ? a.img_id[pb] : 0];
+      const int P = I.N * I.N;
+      const float* Xb = a.X + (size_t)pb * a.xstride;
+      const int p0 = pch * kXT;
+      float* dst = ring + (size_t)slot * D * kXT;
+      for (int it = tid; it < items; it += kXT) {
+        const int r = it / (kXT / 4), q = it - r * (kXT / 4);
+        const int p = p0 + 4 * q;
+        const float* row = Xb + (size_t)r * I.xcstride;
+        const int left = P - p;
+        const uint32_t bytes = left >= 4 ? 16u : (left > 0 ? 4u * left : 0u);
+        cp_async16(dst + r * kXT + 4 * q, bytes ? row + p : row, bytes);
+      }
+      if (++pch == (P + kXT - 1) / kXT) {
+        pb = next_sample(pb);
+        pch = 0;
+      }
+    }
+    cp_async_commit();
+  };
+  for (int s = 0; s < kXRing - 1; ++s) issue(s);
+
+  uint32_t gchunk = 0;
+  for (int b = first; b < a.bs; b = next_sample(b)) {
+    const LsqImage& I = a.img[a.img_id ? a.img_id[b] : 0];
     const int P = I.N * I.N;
-    const float* Xb = a.X + (size_t)b * a.xstride;
-    for (int c = threadIdx.x; c < D; c += kResidThreads) cf[c] = coeffs ? coeffs[(size_t)b * D + c] : 0.f;
-    double acc[kResidChPerWarp];
+    const int nchunks = (P + kXT - 1) / kXT;
+    for (int c = tid; c < D; c += kXT) cf[c] = coeffs[(size_t)b * D + c];
+    float acc_h[kXChPerWarp], acc_l[kXChPerWarp];
 #pragma unroll
-    for (int k = 0; k < kResidChPerWarp; ++k) acc[k] = 0.0;
-    __syncthreads();
-    for (int p0 = 0; p0 < P; p0 += kResidThreads) {
-      const int p = p0 + threadIdx.x;
-      float e = 0.f;
-      if (p < P) {
-        double m = 0.0;
-        if (coeffs)
+    for (int k = 0; k < kXChPerWarp; ++k) acc_h[k] = acc_l[k] = 0.f;
+    float ls = 0.f, cs2 = 0.f;
+    for (int ch = 0; ch < nchunks; ++ch, ++gchunk) {
+      issue((gchunk + kXRing - 1) % kXRing);
+      cp_async_wait<kXRing - 1>();
+      __syncthreads();   // every thread's pieces of this chunk (and cf) are visible
+      const float* xs = ring + (size_t)(gchunk % kXRing) * D * kXT;
+      const int p = ch * kXT + tid;
+      if (IMAGE) {
+        float v = 0.f;
+        for (int c = 0; c < D; ++c) v = fmaf(xs[c * kXT + tid], cf[c], v);
+        if (p < P) {
+          if (img_out) img_out[(size_t)b * a.maxP + p] = v;
+          if (I.obs) {
+            const float err = __ldg(I.err + p);
+            const float zz = (v - __ldg(I.obs + p)) / err;
+            ls += -0.5f * zz * zz - logf(err) - kHalfLog2Pi;
+            cs2 += zz * zz;
+          }
+        }
+      } else {
+        float mh = 0.f, ml = 0.f;
+        if (coeffs) {
           for (int c0 = 0; c0 < D; c0 += 8) {
             float g = 0.f;
-            for (int c = c0; c < min(D, c0 + 8); ++c) g = fmaf(Xb[(size_t)c * I.xcstride + p], cf[c], g);
-            m += (double)g;
+            const int c1 = min(D, c0 + 8);
+            for (int c = c0; c < c1; ++c) g = fmaf(xs[c * kXT + tid], cf[c], g);
+            ff_add(mh, ml, g);
           }
-        const float w = 1.f / I.err[p];
-        e = (float)(((double)I.obs[p] - m) * (double)(w * w));
-      }
-      e_s[threadIdx.x] = e;
-      __syncthreads();
+        }
+        float e = 0.f;
+        if (p < P) {
+          const float w = __ldg(I.W + p);
+          e = ((__ldg(I.obs + p) - mh) - ml) * (w * w);
+        }
+        e_s[tid] = e;
+        __syncthreads();
 #pragma unroll
-      for (int k = 0; k < kResidChPerWarp; ++k) {
-        const int c = warp + k * (kResidThreads / 32);
-        if (c < D) {
-          const float* xc = Xb + (size_t)c * I.xcstride + p0;
-          float g = 0.f;
+        for (int k = 0; k < kXChPerWarp; ++k) {
+          const int c = warp + k * (kXT / 32);
+          if (c < D) {
+            const float* xc = xs + c * kXT;
+            float g = 0.f;
 #pragma unroll
-          for (int j = 0; j < kResidThreads / 32; ++j) {
-            const int q = lane + 32 * j;
-            if (p0 + q < P) g = fmaf(xc[q], e_s[q], g);
+            for (int j = 0; j < kXT / 32; ++j) g = fmaf(xc[lane + 32 * j], e_s[lane + 32 * j], g);
+            ff_add(acc_h[k], acc_l[k], g);
           }
-          acc[k] += (double)g;
         }
       }
-      __syncthreads();
+      __syncthreads();   // the ring slot and e_s are reused next
     }
+    if (IMAGE) {
+      for (int o = 16; o > 0; o >>= 1) {
+        ls += __shfl_xor_sync(0xffffffffu, ls, o);
+        cs2 += __shfl_xor_sync(0xffffffffu, cs2, o);
+      }
+      if (lane == 0) {
+        red[0][warp] = ls;
+        red[1][warp] = cs2;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        float l = 0.f, c = 0.f;
+        for (int w = 0; w < kXT / 32; ++w) {
+          l += red[0][w];
+          c += red[1][w];
+        }
+        if (logL) logL[b] = l;
+        if (chi2) chi2[b] = c / (float)P;
+      }
+      __syncthreads();
+    } else {
 #pragma unroll
-    for (int k = 0; k < kResidChPerWarp; ++k) {
-      const int c = warp + k * (kResidThreads / 32);
-      double v = acc[k];
+      for (int k = 0; k < kXChPerWarp; ++k) {
+        const int c = warp + k * (kXT / 32);
+        double v = (double)acc_h[k] + (double)acc_l[k];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0 && c < D) r[(size_t)b * D + c] = (float)v;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && c < D) r_out[(size_t)b * D + c] = (float)v;
+      }
     }
   }
+  cp_async_wait<0>();
 }
 
 // Refinement step: c += V diag(ilam) V^T r (the pinv of G applied to the residual).
@@ -585,53 +690,15 @@ __global__ void __launch_bounds__(64) lsq_update_kernel(int bs, int D, const flo
   }
 }
 
-__global__ void __launch_bounds__(256) lsq_image_kernel(const __grid_constant__ LsqArgs a,
-                                                        const float* __restrict__ coeffs,
-                                                        float* img_out, float* logL, float* chi2) {
-  __shared__ float cf[kMaxLsqChannels];
-  __shared__ float red[2][8];
-  for (int b = blockIdx.x; b < a.bs; b += gridDim.x) {
-    const int im = a.img_id ? a.img_id[b] : 0;
-    if (im < 0 || im >= a.n_images) continue;
-    const LsqImage& I = a.img[im];
-    const int P = I.N * I.N;
-    for (int c = threadIdx.x; c < a.D; c += blockDim.x) cf[c] = coeffs[(size_t)b * a.D + c];
-    __syncthreads();
-    const float* Xb = a.X + (size_t)b * a.xstride;
-    float ls = 0.f, cs2 = 0.f;
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
-      float v = 0.f;
-      for (int c = 0; c < a.D; ++c) v = fmaf(Xb[(size_t)c * I.xcstride + p], cf[c], v);
-      if (img_out) img_out[(size_t)b * a.maxP + p] = v;
-      if (I.obs) {
-        const float err = I.err[p];
-        const float zz = (v - I.obs[p]) / err;
-        ls += -0.5f * zz * zz - logf(err) - kHalfLog2Pi;
-        cs2 += zz * zz;
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      ls += __shfl_xor_sync(0xffffffffu, ls, o);
-      cs2 += __shfl_xor_sync(0xffffffffu, cs2, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-      red[0][threadIdx.x >> 5] = ls;
-      red[1][threadIdx.x >> 5] = cs2;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      float l = 0.f, c = 0.f;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-        l += red[0][w];
-        c += red[1][w];
-      }
-      if (logL) logL[b] = l;
-      if (chi2) chi2[b] = c / (float)P;
-    }
-    __syncthreads();
+// W = 1 / err and b = W * obs per image, zero beyond the N^2 pixels.
+__global__ void lsq_weights_kernel(const float* __restrict__ err, const float* __restrict__ obs, int P,
+                                   int padded, float* __restrict__ W, float* __restrict__ bw) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < padded; p += gridDim.x * blockDim.x) {
+    const float w = p < P ? 1.f / err[p] : 0.f;
+    W[p] = w;
+    bw[p] = p < P && obs ? obs[p] * w : 0.f;
   }
 }
-
 // ------------------------------------------------------------------ host side
 static int g_lsq_smem_set[kMaxDevices];   // basis kernel smem attribute set per device
 
@@ -673,7 +740,11 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
       int n1 = 0, n2 = 0;
       const int nl = (p.niter + 1) * (p.niter + 2) / 2;
       for (int k = 0; k < nl; ++k) {
-        if (D >= kMaxLsqChannels) break;
+        if (D >= kMaxLsqChannels) {
+          set_error("least squares: more than %d basis channels", kMaxLsqChannels);
+          delete L;
+          return GL_ERR_UNSUPPORTED;
+        }
         L->ch[D].kind = 1;
         L->ch[D].prof = L->n_prof;
         L->ch[D].n1 = n1;
@@ -696,7 +767,11 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
         pr.col[4] = p.col[2];
         pr.col[5] = p.col[3];
       }
-      if (D >= kMaxLsqChannels) break;
+      if (D >= kMaxLsqChannels) {
+        set_error("least squares: more than %d basis channels", kMaxLsqChannels);
+        delete L;
+        return GL_ERR_UNSUPPORTED;
+      }
       L->ch[D].kind = 0;
       L->ch[D].prof = L->n_prof;
       ++D;
@@ -721,7 +796,7 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
   int dev_smem = 0;
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
   const int static_bytes = 8 * 1024;
-  int maxP = 0, smem = 0, max_bands = 0;
+  int maxP = 0, maxXc = 0, smem = 0, max_bands = 0;
   size_t beta_per_cta = 0;
   for (int i = 0; i < plan->n_images; ++i) {
     const DevImage& F = plan->img[i];
@@ -739,7 +814,7 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
     I.grid = F.grid;
     I.kern = F.kern;
     I.obs = F.obs;
-    I.xcstride = F.N * F.N;
+    I.xcstride = (F.N * F.N + 3) & ~3;   // 16-byte aligned channel rows (cp.async)
     I.cpass = D;
     int dmin = F.d[0], dmax = F.d[0];
     for (int p = 1; p < F.ss; ++p) {
@@ -805,17 +880,23 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
     if (beta_n > beta_per_cta) beta_per_cta = beta_n;
     if (I.smem_floats * 4 > smem) smem = I.smem_floats * 4;
     if (F.N * F.N > maxP) maxP = F.N * F.N;
+    if (I.xcstride > maxXc) maxXc = I.xcstride;
     if (I.nbands > max_bands) max_bands = I.nbands;
   }
   L->smem_bytes = smem;
   L->maxP = maxP;
+  L->maxXc = maxXc;
   L->max_bands = max_bands;
   L->beta_per_cta = beta_per_cta;
   L->n_sm = 1;
   cudaDeviceGetAttribute(&L->n_sm, cudaDevAttrMultiProcessorCount, plan->device);
-  // error maps on the device
+  // error maps, W = 1/err and b = W * obs on the device (W and b zero-padded
+  // to whole streaming chunks)
+  auto up256 = [](size_t v) { return (v + 255) / 256 * 256; };
+  auto padded = [](size_t P) { return (P + kPixPad - 1) / kPixPad * kPixPad; };
   size_t bytes = 0;
-  for (int i = 0; i < plan->n_images; ++i) bytes += ((size_t)errs[i].size() * 4 + 255) / 256 * 256;
+  for (int i = 0; i < plan->n_images; ++i)
+    bytes += up256(errs[i].size() * 4) + 2 * up256(padded(errs[i].size()) * 4);
   if (cudaMalloc((void**)&L->dev_err, bytes) != cudaSuccess) {
     set_error("cudaMalloc(error maps) failed");
     delete L;
@@ -823,9 +904,33 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
   }
   char* base = (char*)L->dev_err;
   for (int i = 0; i < plan->n_images; ++i) {
-    cudaMemcpy(base, errs[i].data(), errs[i].size() * 4, cudaMemcpyHostToDevice);
-    L->img[i].err = (const float*)base;
-    base += ((size_t)errs[i].size() * 4 + 255) / 256 * 256;
+    const size_t P = errs[i].size(), Pp = padded(P);
+    cudaMemcpy(base, errs[i].data(), P * 4, cudaMemcpyHostToDevice);
+    LsqImage& I = L->img[i];
+    I.err = (const float*)base;
+    base += up256(P * 4);
+    float* W = (float*)base;
+    base += up256(Pp * 4);
+    float* bw = (float*)base;
+    base += up256(Pp * 4);
+    lsq_weights_kernel<<<(int)((Pp + 255) / 256), 256>>>(I.err, I.obs, (int)P, (int)Pp, W, bw);
+    I.W = W;
+    I.bw = bw;
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    set_error("least squares weights: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaFree(L->dev_err);
+    delete L;
+    return GL_ERR_CUDA;
+  }
+  if (cudaFuncSetAttribute(lsq_xpass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)xpass_smem_bytes(D)) != cudaSuccess ||
+      cudaFuncSetAttribute(lsq_xpass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)xpass_smem_bytes(D)) != cudaSuccess) {
+    set_error("least squares pass kernels: shared memory attribute: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaFree(L->dev_err);
+    delete L;
+    return GL_ERR_CUDA;
   }
   const int dev_slot = current_device_slot();
   if (smem > g_lsq_smem_set[dev_slot]) {
@@ -856,11 +961,11 @@ static int basis_ctas(const LsqPlan* L, int bs) {
   return (int)std::max(1LL, std::min(items, (long long)L->n_sm));
 }
 
-// Workspace: X [bs][D][maxP], G [bs][D][D], V [bs][D][D], h, r, ilam [bs][D],
+// Workspace: X [bs][D][maxXc], G [bs][D][D], V [bs][D][D], h, r, ilam [bs][D],
 // beta [basis CTAs][beta_per_cta] (float2), status.
 size_t lsq_status_offset(const LsqPlan* L, int bs) {
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
-  const size_t X = (size_t)bs * L->D * L->maxP * 4;
+  const size_t X = (size_t)bs * L->D * L->maxXc * 4;
   const size_t G = (size_t)bs * L->D * L->D * 4;
   const size_t h = (size_t)bs * L->D * 4;
   const size_t beta = (size_t)basis_ctas(L, bs) * L->beta_per_cta * 8;
@@ -896,11 +1001,11 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   a.img_id = img_id;
   a.maxP = L->maxP;
   a.max_bands = L->max_bands;
-  a.xstride = (size_t)L->D * L->maxP;
+  a.xstride = (size_t)L->D * L->maxXc;
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   char* base = (char*)work;
   a.X = (float*)base;
-  base += up((size_t)bs * L->D * L->maxP * 4);
+  base += up((size_t)bs * L->D * L->maxXc * 4);
   float* G = (float*)base;
   base += up((size_t)bs * L->D * L->D * 4);
   float* V = (float*)base;
@@ -928,22 +1033,23 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   int sms = 1;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
   cudaMemsetAsync(status, 0, sizeof(int), stream);
-  // basis stack, then G = A^T A on the tensor cores (3xTF32)
+  // basis stack, then G = A^T A and h = A^T b on the tensor cores (3xTF32)
   lsq_basis_kernel<<<n_basis, kThreads, L->smem_bytes, stream>>>(a);
-  int rc = launch_gram_tc(a, G, status, bs < 2 * sms ? bs : 2 * sms, stream);
+  const int gram_grid = std::min(bs, gram_tc_ctas_per_sm(L->D) * sms);
+  int rc = launch_gram_tc(a, G, h, status, gram_grid, stream);
   if (rc) return rc;
-  // h = A^T b from the basis, c0 = pinv(G) h, then two refinement steps
-  // against the residual of the least-squares problem itself
-  const int resid_blocks = bs < 8 * sms ? bs : 8 * sms;
-  lsq_resid_kernel<<<resid_blocks, kResidThreads, 0, stream>>>(a, nullptr, h);
+  // c0 = pinv(G) h, then two refinement steps against the residual of the
+  // least-squares problem itself
+  const int xpass_blocks = std::min(bs, sms);
+  const size_t xsm = xpass_smem_bytes(L->D);
   lsq_solve_kernel<<<bs < 8 * sms ? bs : 8 * sms, 128, 0, stream>>>(bs, L->D, G, h, 1e-6f, co, 30, V, ilam,
                                                                   status);
   for (int it = 0; it < 2; ++it) {
-    lsq_resid_kernel<<<resid_blocks, kResidThreads, 0, stream>>>(a, co, r);
+    lsq_xpass_kernel<false><<<xpass_blocks, kXT, xsm, stream>>>(a, co, r, nullptr, nullptr, nullptr);
     lsq_update_kernel<<<bs < 8 * sms ? bs : 8 * sms, 64, 0, stream>>>(bs, L->D, V, ilam, r, co);
   }
   if (img_out || logL || chi2)
-    lsq_image_kernel<<<bs < 4 * sms ? bs : 4 * sms, 256, 0, stream>>>(a, co, img_out, logL, chi2);
+    lsq_xpass_kernel<true><<<xpass_blocks, kXT, xsm, stream>>>(a, co, nullptr, img_out, logL, chi2);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error("least squares launch: %s", cudaGetErrorString(e));

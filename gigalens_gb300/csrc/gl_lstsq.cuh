@@ -7,7 +7,8 @@
 
 namespace gl {
 
-constexpr int kMaxLsqChannels = 64;   // basis images per sample (shapelets n_max <= 9 + lens light)
+constexpr int kMaxLsqChannels = 63;   // basis images per sample (shapelets n_max <= 9 + lens light);
+                                      // with the data row b the normal equations have <= 64 rows
 constexpr int kMaxLsqProfiles = 4;
 
 struct LsqChannel {
@@ -34,14 +35,18 @@ struct LsqImage {
   int brows;          // plane rows held per band: Bo + KS + R0 - min_p d[p]
   int nbands;
   int cpass;          // number of channels (D)
-  int xcstride;       // floats between channels in X (N*N)
+  int xcstride;       // floats between channels in X (N*N rounded up to a multiple of 4)
   int plane_floats;   // brows * pitch
   int offK, smem_floats;
   const float* grid;
   const float* kern;
   const float* obs;
   const float* err;
+  const float* W;     // 1 / err, zero-padded to a multiple of kPixPad floats
+  const float* bw;    // b = W * obs, zero-padded likewise
 };
+
+constexpr int kPixPad = 256;   // pixel padding of W and bw (the streaming kernels' chunk)
 
 struct LsqArgs {
   int bs, d, D, n_images, n_prof, has_shear;
@@ -61,6 +66,7 @@ struct LsqArgs {
 
 struct LsqPlan {
   int D, n_prof, has_shear, maxP, max_bands, smem_bytes;
+  int maxXc;            // largest per-channel stride of X (floats)
   int n_sm;             // CTAs of the basis kernel at most (one per SM)
   size_t beta_per_cta;  // float2 of the largest band's ray-traced coordinates
   LsqProfile prof[kMaxLsqProfiles];
@@ -72,8 +78,9 @@ struct LsqPlan {
 
 int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs);
 // tensor-core Gram (gl_gram_tc.cu)
-int launch_gram_tc(const LsqArgs& a, float* G, int* status, int grid, cudaStream_t stream);
-int gram_tc_smem_bytes();
+int launch_gram_tc(const LsqArgs& a, float* G, float* h, int* status, int grid, cudaStream_t stream);
+int gram_tc_smem_bytes(int D);
+int gram_tc_ctas_per_sm(int D);
 void set_gram_wait_polls(int polls);   // < 0: the default limit
 size_t lsq_status_offset(const LsqPlan* L, int bs);
 void lsq_destroy(gl_plan* plan);
