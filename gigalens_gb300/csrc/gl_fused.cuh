@@ -253,10 +253,11 @@ static __device__ void phase_conv_forward(const DevImage& I, float* sm, float* i
       const float* plane = sm + I.offI + pq * I.N * I.pitchI + I.padI[q] - I.d[q] + j0;
       const float* kp = sm + I.offK + pq * KS * I.ksp;
       const int mlo = max(0, I.d[p] - i), mhi = min(KS, I.N + I.d[p] - i);
-      // the prefetch one row past mhi reads the next plane, the likelihood
-      // plane or the sub-kernels: all inside shared memory
-      corr_rows<KS, false, kFusedCB>(plane + (i + mlo - I.d[p]) * I.pitchI, I.pitchI, kp + mlo * I.ksp,
-                                     I.ksp, mhi - mlo, acc);
+      CorrX2Acc<kFusedCB> A;
+      A.zero();
+      corr_rows_x2<KS, false, kFusedCB>(plane + (i + mlo - I.d[p]) * I.pitchI, I.pitchI, kp + mlo * I.ksp,
+                                        I.ksp, mhi - mlo, A);
+      A.finish(acc);
     }
     if (I.nplanes == 4) {
       float r8[8], r4[4];
@@ -332,16 +333,18 @@ static __device__ void phase_conv_adjoint(const DevImage& I, float* sm) {
     const int mlo = max(0, ep - Y), mhi = min(KS, I.N + ep - Y);
     const float* row0 = wb + (Y + mlo - ep) * I.pitchW;
     const float* k0 = kp + (KS - 1 - mlo) * I.ksp;
-    // the prefetch one row past mhi reads the spare row after the plane
+    CorrX2Acc<kFusedCB> A;
+    A.zero();
     if constexpr (KS % 2 == 0) {
       if (I.d[q] != I.d[0]) {
-        corr_rows<KS, true, kFusedCB, 1>(row0 - 1, I.pitchW, k0, -I.ksp, mhi - mlo, acc);
+        corr_rows_x2<KS, true, kFusedCB, 1>(row0 - 1, I.pitchW, k0, -I.ksp, mhi - mlo, A);
       } else {
-        corr_rows<KS, true, kFusedCB, 0>(row0, I.pitchW, k0, -I.ksp, mhi - mlo, acc);
+        corr_rows_x2<KS, true, kFusedCB, 0>(row0, I.pitchW, k0, -I.ksp, mhi - mlo, A);
       }
     } else {
-      corr_rows<KS, true, kFusedCB, 0>(row0, I.pitchW, k0, -I.ksp, mhi - mlo, acc);
+      corr_rows_x2<KS, true, kFusedCB, 0>(row0, I.pitchW, k0, -I.ksp, mhi - mlo, A);
     }
+    A.finish(acc);
     float* dst = sm + I.offI + pq * I.N * I.pitchI + Y * I.pitchI + I.padI[q] + j0;
 #pragma unroll
     for (int c = 0; c < kFusedCB; ++c)

@@ -137,16 +137,17 @@ __device__ void lsq_pass_conv(const LsqImage& I, const float* sm, int c0, int nb
     const int cb = rest - slot * I.ncbC;
     if (c0 + slot >= I.cpass) continue;
     const int j0 = cb * CB;
-    float acc[CB];
-#pragma unroll
-    for (int c = 0; c < CB; ++c) acc[c] = 0.f;
+    CorrX2Acc<CB> A;
+    A.zero();
     const float* sbase = sm + (size_t)slot * I.nplanes * I.plane_floats + j0;
     for (int pq = 0; pq < I.nplanes; ++pq) {
       const int p = pq / I.ss;
       // output row i0 + il of parity p reads plane rows i0 + il - d[p] + m
       const float* seg = sbase + pq * I.plane_floats + (il + I.R0 - I.d[p]) * I.pitch;
-      corr_rows<KS, false, CB>(seg, I.pitch, kern + pq * KS * I.ksp, I.ksp, KS, acc);
+      corr_rows_x2<KS, false, CB>(seg, I.pitch, kern + pq * KS * I.ksp, I.ksp, KS, A);
     }
+    float acc[CB];
+    A.finish(acc);
     float* dst = Xout + (size_t)(c0 + slot) * I.xcstride + (size_t)(i0 + il) * I.N + j0;
 #pragma unroll
     for (int c = 0; c < CB; ++c)
