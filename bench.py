@@ -243,7 +243,7 @@ def _events(torch, n):
     return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
 
 
-def lstsq_workload(torch, dev, n_big=2048, n_small=512):
+def lstsq_workload(torch, dev, n_big=2048, n_small=512, tuning=None):
     """The least-squares configuration: EPL + shear lens, shapelet source with
     n_max = 8 (45 channels) solved linearly, n_big samples of a 100x100 image
     and n_small of a 60x60 image in one uneven launch.  Returns a callable
@@ -272,6 +272,11 @@ def lstsq_workload(torch, dev, n_big=2048, n_small=512):
     xs = [[lens[0], lens[1]], [{k: torch.tensor(v, dtype=torch.float32) for k, v in cols.items()}]]
     x = lay.flatten_params(xs)
     img_id = torch.cat([torch.zeros(n_big, dtype=torch.int32), torch.ones(n_small, dtype=torch.int32)]).to(dev)
+    from gigalens_gb300.cuda import autotune
+    if tuning:   # a fixed launch shape instead of the tuner's choice
+        autotune.set_tuning(lplan, lsq_ctas_per_sm=tuning[0], lsq_col_block=tuning[1])
+    else:        # the tuner's choice (timed on these inputs on first use, then cached)
+        autotune.ensure_lstsq(lplan, x, img_id)
     wb, D = ctypes.c_size_t(0), ctypes.c_int(0)
     N.call("gl_lstsq_workspace", lplan.handle, nb, ctypes.byref(wb), ctypes.byref(D))
     work = torch.empty(wb.value, dtype=torch.uint8, device=dev)
@@ -283,6 +288,8 @@ def lstsq_workload(torch, dev, n_big=2048, n_small=512):
                N.ptr(lg), None, N.stream_ptr())
 
     lsq.plan = lplan
+    lsq.inputs = (x, img_id)
+    lsq.tuning = autotune.get_tuning(lplan)
     return lsq, nb, wb, work
 
 
@@ -292,7 +299,8 @@ def run_lstsq_only(args):
 
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    lsq, nb, wb, work = lstsq_workload(torch, dev, args.lstsq_big, args.lstsq_small)
+    tuning = (args.lstsq_ctas, args.lstsq_cb) if (args.lstsq_ctas or args.lstsq_cb) else None
+    lsq, nb, wb, work = lstsq_workload(torch, dev, args.lstsq_big, args.lstsq_small, tuning)
     for _ in range(args.warmup):
         lsq()
     torch.cuda.synchronize()
@@ -306,7 +314,7 @@ def run_lstsq_only(args):
     print(json.dumps({"metric": "lstsq evals/s (%d x 100^2 + %d x 60^2 px, ss=2, shapelets n_max=8, D=45)"
                                 % (args.lstsq_big, args.lstsq_small),
                       "value": nb / (t * 1e-3), "unit": "evals/s", "ms_per_step": t, "steps": args.steps,
-                      "warmup": args.warmup, "workspace_gb": wb.value / 1e9}), flush=True)
+                      "warmup": args.warmup, "workspace_gb": wb.value / 1e9, "tuning": lsq.tuning}), flush=True)
 
 
 def run_sequence(args):
@@ -457,6 +465,7 @@ def secondary_timings(torch, dev, pm, plan, z):
     out["lstsq_ms_2048x100px_plus_512x60px"] = t
     out["lstsq_evals_per_s"] = nb / (t * 1e-3)
     out["lstsq_workspace_gb"] = wb.value / 1e9
+    out["lstsq_tuning"] = lsq.tuning
     del work
 
     # one fixed-length HMC iteration: 2048 chains x 8 leapfrog launches
@@ -494,6 +503,7 @@ def run_ours(args):
 
     from gigalens_gb300 import _native as N
     from gigalens_gb300 import workloads as W
+    from gigalens_gb300.cuda import autotune
     from gigalens_gb300.cuda.model import ForwardProbModel, log_prob_and_grad
     from gigalens_gb300.cuda.simulator import LensSimulator
 
@@ -616,7 +626,7 @@ def run_ours(args):
                                        "forward+adjoint launch per step" % (bs, n_pix, n_pix, psf, psf),
                            "chains_per_gpu": bs, "epl_terms": K, "l2": "flushed between steps (256 MiB write)",
                            "image_planes": "global memory (L2)" if lc["global_planes"] else "shared memory",
-                           "wall_s_timed": t_wall, "finite": finite},
+                           "wall_s_timed": t_wall, "finite": finite, "tuning": autotune.get_tuning(plan)},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(z.numel() * 4),
                         "d2h_bytes_per_step": int(out_host.numel() * 4),
                         "api": "ForwardProbModel.log_prob + torch.autograd.grad, pinned host buffers"},
@@ -664,6 +674,8 @@ def main():
                     help="time only the least-squares configuration (for profiling)")
     ap.add_argument("--lstsq-big", type=int, default=2048, help="samples of the 100x100 image")
     ap.add_argument("--lstsq-small", type=int, default=512, help="samples of the 60x60 image")
+    ap.add_argument("--lstsq-ctas", type=int, default=0, help="basis kernel CTAs per SM (1 or 2; 0: plan default)")
+    ap.add_argument("--lstsq-cb", type=int, default=0, help="basis correlation column block (16, 20; 0: planner)")
     ap.add_argument("--sequence", action="store_true",
                     help="run the full MAP -> SVI -> HMC sequence at 90^2 px (about two minutes)")
     ap.add_argument("--seq-map-chains", type=int, default=4096)

@@ -94,6 +94,11 @@ class gl_tune_result(ctypes.Structure):
                                             "family", "global_planes", "subkernel_side", "col_block")]
 
 
+class gl_tuning(ctypes.Structure):
+    _fields_ = [("lsq_ctas_per_sm", ctypes.c_int), ("lsq_col_block", ctypes.c_int),
+                ("fused_corr", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+
+
 class gl_image_desc(ctypes.Structure):
     _fields_ = [
         ("num_pix", ctypes.c_int),
@@ -167,6 +172,8 @@ SIGNATURES = [
     ("gl_lstsq_status", _i, [_vp, _i, _vp, _vp, _vp]),
     ("gl_test_set_wait_polls", _i, [_i]),
     ("gl_autotune", _i, [_vp, _i, _vp]),
+    ("gl_plan_set_tuning", _i, [_vp, ctypes.POINTER(gl_tuning)]),
+    ("gl_plan_get_tuning", _i, [_vp, ctypes.POINTER(gl_tuning)]),
     ("gl_nn_gemm", _i, [_i, _i, _i, _i, _i, _i, ctypes.c_float, _vp, _i, ctypes.c_longlong, _vp, _i,
                         ctypes.c_longlong, ctypes.c_float, _vp, _i, ctypes.c_longlong, _i, _i, _vp]),
     ("gl_nn_im2col3x3", _i, [_vp, _i, _i, _i, _i, _i, _vp, _vp]),

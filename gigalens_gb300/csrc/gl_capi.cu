@@ -406,6 +406,7 @@ static DevPriorLeaf make_leaf(const gl_prior_leaf& l) {
 static void fill_args(const gl_plan* plan, FusedArgs& a) {
   memset(&a, 0, sizeof(a));
   a.family = plan->family;
+  a.corr_scalar = plan->corr_scalar;
   a.d = plan->model.n_params;
   a.n_images = plan->n_images;
   for (int i = 0; i < plan->n_images; ++i) a.img[i] = plan->img[i];
@@ -438,6 +439,7 @@ int gl_struct_size(int which) {
     case 3: return (int)sizeof(gl_prior_leaf);
     case 4: return (int)sizeof(gl_tune_result);
     case 5: return (int)sizeof(gl_adam_cfg);
+    case 6: return (int)sizeof(gl_tuning);
     default: return -1;
   }
 }

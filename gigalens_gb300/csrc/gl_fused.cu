@@ -25,6 +25,7 @@ int fused_kernel_prepare(int smem_bytes) {
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SHEAR_SE>(smem_bytes);
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SE_SE>(smem_bytes);
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SE>(smem_bytes);
+  if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SHEAR_SE_SE, false>(smem_bytes);
   if (e != cudaSuccess) {
     set_error("cudaFuncSetAttribute(max dynamic smem %d): %s", smem_bytes, cudaGetErrorString(e));
     return GL_ERR_CUDA;
@@ -56,7 +57,12 @@ int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream) {
     }
   } else {
     switch (a.family) {
-      case FAM_EPL_SHEAR_SE_SE: fam_launch<FAM_EPL_SHEAR_SE_SE, false>(a, grid, smem_bytes, stream); break;
+      case FAM_EPL_SHEAR_SE_SE:
+        if (a.corr_scalar)
+          fam_launch<FAM_EPL_SHEAR_SE_SE, false, false>(a, grid, smem_bytes, stream);
+        else
+          fam_launch<FAM_EPL_SHEAR_SE_SE, false>(a, grid, smem_bytes, stream);
+        break;
       case FAM_EPL_SHEAR_SE: fam_launch<FAM_EPL_SHEAR_SE, false>(a, grid, smem_bytes, stream); break;
       case FAM_EPL_SE_SE: fam_launch<FAM_EPL_SE_SE, false>(a, grid, smem_bytes, stream); break;
       case FAM_EPL_SE: fam_launch<FAM_EPL_SE, false>(a, grid, smem_bytes, stream); break;

@@ -208,7 +208,7 @@ __device__ __forceinline__ bool conv_unit(const DevImage& I, int item, int lane,
 // With four planes the quarter-warps' partial outputs are combined by a
 // reduce-scatter in a fixed order: quarter j ends with outputs 4j..4j+3 of
 // its 16-column block, (a_j + a_{j^2}) + (a_{j^1} + a_{j^3}).
-template <int KS>
+template <int KS, bool X2>
 static __device__ void phase_conv_forward(const DevImage& I, float* sm, float* img_out, bool want_w,
                                    const float* err_map, float cf, float& lsum, float& csum) {
   const int lane = threadIdx.x & 31, qtr = lane >> 3;
@@ -253,11 +253,18 @@ static __device__ void phase_conv_forward(const DevImage& I, float* sm, float* i
       const float* plane = sm + I.offI + pq * I.N * I.pitchI + I.padI[q] - I.d[q] + j0;
       const float* kp = sm + I.offK + pq * KS * I.ksp;
       const int mlo = max(0, I.d[p] - i), mhi = min(KS, I.N + I.d[p] - i);
-      CorrX2Acc<kFusedCB> A;
-      A.zero();
-      corr_rows_x2<KS, false, kFusedCB>(plane + (i + mlo - I.d[p]) * I.pitchI, I.pitchI, kp + mlo * I.ksp,
-                                        I.ksp, mhi - mlo, A);
-      A.finish(acc);
+      if constexpr (X2) {
+        CorrX2Acc<kFusedCB> A;
+        A.zero();
+        corr_rows_x2<KS, false, kFusedCB>(plane + (i + mlo - I.d[p]) * I.pitchI, I.pitchI, kp + mlo * I.ksp,
+                                          I.ksp, mhi - mlo, A);
+        A.finish(acc);
+      } else {
+        // the prefetch one row past mhi reads the next plane, the likelihood
+        // plane or the sub-kernels: all inside shared memory
+        corr_rows<KS, false, kFusedCB>(plane + (i + mlo - I.d[p]) * I.pitchI, I.pitchI, kp + mlo * I.ksp,
+                                       I.ksp, mhi - mlo, acc);
+      }
     }
     if (I.nplanes == 4) {
       float r8[8], r4[4];
@@ -315,7 +322,7 @@ static __device__ __forceinline__ bool adj_unit(const DevImage& I, int item, int
 }
 
 // Phase 3: transposed correlation, adjoint image -> supersampled parity planes.
-template <int KS>
+template <int KS, bool X2>
 static __device__ void phase_conv_adjoint(const DevImage& I, float* sm) {
   const int lane = threadIdx.x & 31;
   const int items = adj_items(I);
@@ -333,18 +340,31 @@ static __device__ void phase_conv_adjoint(const DevImage& I, float* sm) {
     const int mlo = max(0, ep - Y), mhi = min(KS, I.N + ep - Y);
     const float* row0 = wb + (Y + mlo - ep) * I.pitchW;
     const float* k0 = kp + (KS - 1 - mlo) * I.ksp;
-    CorrX2Acc<kFusedCB> A;
-    A.zero();
-    if constexpr (KS % 2 == 0) {
-      if (I.d[q] != I.d[0]) {
-        corr_rows_x2<KS, true, kFusedCB, 1>(row0 - 1, I.pitchW, k0, -I.ksp, mhi - mlo, A);
+    if constexpr (X2) {
+      CorrX2Acc<kFusedCB> A;
+      A.zero();
+      if constexpr (KS % 2 == 0) {
+        if (I.d[q] != I.d[0]) {
+          corr_rows_x2<KS, true, kFusedCB, 1>(row0 - 1, I.pitchW, k0, -I.ksp, mhi - mlo, A);
+        } else {
+          corr_rows_x2<KS, true, kFusedCB, 0>(row0, I.pitchW, k0, -I.ksp, mhi - mlo, A);
+        }
       } else {
         corr_rows_x2<KS, true, kFusedCB, 0>(row0, I.pitchW, k0, -I.ksp, mhi - mlo, A);
       }
+      A.finish(acc);
     } else {
-      corr_rows_x2<KS, true, kFusedCB, 0>(row0, I.pitchW, k0, -I.ksp, mhi - mlo, A);
+      // the prefetch one row past mhi reads the spare row after the plane
+      if constexpr (KS % 2 == 0) {
+        if (I.d[q] != I.d[0]) {
+          corr_rows<KS, true, kFusedCB, 1>(row0 - 1, I.pitchW, k0, -I.ksp, mhi - mlo, acc);
+        } else {
+          corr_rows<KS, true, kFusedCB, 0>(row0, I.pitchW, k0, -I.ksp, mhi - mlo, acc);
+        }
+      } else {
+        corr_rows<KS, true, kFusedCB, 0>(row0, I.pitchW, k0, -I.ksp, mhi - mlo, acc);
+      }
     }
-    A.finish(acc);
     float* dst = sm + I.offI + pq * I.N * I.pitchI + Y * I.pitchI + I.padI[q] + j0;
 #pragma unroll
     for (int c = 0; c < kFusedCB; ++c)
@@ -1050,7 +1070,8 @@ static __device__ void setup_image(const DevImage& I, float* sm) {
   for (int i = threadIdx.x; i < nk; i += kThreads) sm[I.offK + i] = __ldg(I.kern + i);
 }
 
-template <int FAM, bool GMEM>
+// X2: PSF correlations on packed FFMA2 (corr_rows_x2) or scalar FFMA (corr_rows).
+template <int FAM, bool GMEM, bool X2>
 __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constant__ FusedArgs a) {
   extern __shared__ float4 smem_dyn[];
   // the image planes: dynamic shared memory, or (GMEM) this CTA's slice of a
@@ -1132,7 +1153,7 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
     const float* err_map = (FAM == FAM_GENERIC && a.gen.noise_err) ? I.err : nullptr;
     const float cf = (FAM == FAM_GENERIC && a.gen.unit_cf) ? 1.f : I.cf;
 #define GL_CALL_FWD(KSV) \
-  phase_conv_forward<KSV>(I, sm, img_out, a.want_grad != 0, err_map, cf, lsum, csum)
+  phase_conv_forward<KSV, X2>(I, sm, img_out, a.want_grad != 0, err_map, cf, lsum, csum)
     GL_KS_DISPATCH(I.KS, GL_CALL_FWD)
 #undef GL_CALL_FWD
     {
@@ -1144,7 +1165,7 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
     __syncthreads();   // st.out is reused by the gradient reduction
 
     if (a.want_grad) {
-#define GL_CALL_ADJ(KSV) phase_conv_adjoint<KSV>(I, sm)
+#define GL_CALL_ADJ(KSV) phase_conv_adjoint<KSV, X2>(I, sm)
       GL_KS_DISPATCH(I.KS, GL_CALL_ADJ)
 #undef GL_CALL_ADJ
       __syncthreads();
@@ -1200,7 +1221,7 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
 // ---------------------------------------------------------------- host entries
 // Defined here, instantiated once per family in gl_fused_fam*.cu so that the
 // families compile as separate translation units (in parallel).
-template <int FAM, bool GMEM>
+template <int FAM, bool GMEM, bool X2>
 int fam_launch(const FusedArgs& a, int grid, int smem_bytes, cudaStream_t stream) {
   if constexpr (GMEM) {
     // no dynamic shared memory: give the SM's unified memory to L1, which
@@ -1208,24 +1229,25 @@ int fam_launch(const FusedArgs& a, int grid, int smem_bytes, cudaStream_t stream
     static bool carveout_set[kMaxDevices];
     const int dev = current_device_slot();
     if (!carveout_set[dev])
-      carveout_set[dev] = cudaFuncSetAttribute(fused_kernel<FAM, true>,
+      carveout_set[dev] = cudaFuncSetAttribute(fused_kernel<FAM, true, X2>,
                                                cudaFuncAttributePreferredSharedMemoryCarveout,
                                                (int)cudaSharedmemCarveoutMaxL1) == cudaSuccess;
   }
-  fused_kernel<FAM, GMEM><<<grid, kThreads, GMEM ? 0 : smem_bytes, stream>>>(a);
+  fused_kernel<FAM, GMEM, X2><<<grid, kThreads, GMEM ? 0 : smem_bytes, stream>>>(a);
   return 0;
 }
 
-template <int FAM>
+template <int FAM, bool X2>
 cudaError_t fam_set_smem(int smem_bytes) {
-  return cudaFuncSetAttribute(fused_kernel<FAM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  return cudaFuncSetAttribute(fused_kernel<FAM, false, X2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              smem_bytes);
 }
 
 // (the general path exists only with global planes)
 template <int FAM>
 int fam_static_smem() {
   cudaFuncAttributes at;
-  if (cudaFuncGetAttributes(&at, fused_kernel<FAM, FAM == FAM_GENERIC>) != cudaSuccess) {
+  if (cudaFuncGetAttributes(&at, fused_kernel<FAM, FAM == FAM_GENERIC, true>) != cudaSuccess) {
     cudaGetLastError();
     return (int)sizeof(SmemStatic);
   }

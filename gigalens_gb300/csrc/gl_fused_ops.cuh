@@ -4,9 +4,9 @@
 #include "gl_internal.cuh"
 
 namespace gl {
-template <int FAM, bool GMEM>
+template <int FAM, bool GMEM, bool X2 = true>
 int fam_launch(const FusedArgs& a, int grid, int smem_bytes, cudaStream_t stream);
-template <int FAM>
+template <int FAM, bool X2 = true>
 cudaError_t fam_set_smem(int smem_bytes);
 template <int FAM>
 int fam_static_smem();

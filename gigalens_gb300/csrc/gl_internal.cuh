@@ -130,6 +130,7 @@ struct FusedArgs {
   float* gscratch;          // images too large for shared memory: per-CTA planes in
   int cta_floats;           //   global memory (cta_floats per CTA), else null
   int n_cta;                //   slices in gscratch: the grid never exceeds it
+  int corr_scalar;          // 1: the headline family's scalar-FFMA correlation variant
 };
 
 }  // namespace gl
@@ -155,6 +156,7 @@ struct gl_plan {
   int cta_floats;           // floats per CTA in gscratch
   int n_cta;                // CTAs gscratch holds (the device's SM count)
   void* lsq;                // gl::LsqPlan of the least-squares path, or null
+  int corr_scalar;          // tuning: scalar-FFMA correlations in the headline family
   const float* shp_tab;     // shapelet table (interpolating shapelet profiles), or null
 };
 

@@ -80,15 +80,16 @@ constexpr int kEvalU = 4;   // pixels per thread and iteration in the channel ev
 struct LsqShared {
   float x[GL_MAX_PARAMS];
   float4 tab[kMaxTerms + 2];
-  float red[kThreads / 32][4];
+  float red[16][4];   // per warp (at most 16)
   int K[GL_MAX_IMAGES];
 };
 
+template <int NT>
 __device__ void lsq_term_counts(const LsqArgs& a, LsqShared& st) {
   float mx[GL_MAX_IMAGES];
   for (int i = 0; i < GL_MAX_IMAGES; ++i) mx[i] = 0.f;
   const int c1 = a.epl.col[2], c2 = a.epl.col[3];
-  for (int b = threadIdx.x; b < a.bs; b += kThreads) {
+  for (int b = threadIdx.x; b < a.bs; b += NT) {
     const int im = a.img_id ? a.img_id[b] : 0;
     const float e1 = c1 >= 0 ? a.x[(size_t)b * a.d + c1] : 0.f;
     const float e2 = c2 >= 0 ? a.x[(size_t)b * a.d + c2] : 0.f;
@@ -105,7 +106,7 @@ __device__ void lsq_term_counts(const LsqArgs& a, LsqShared& st) {
     __syncthreads();
     if (threadIdx.x == 0) {
       float t = 0.f;
-      for (int w = 0; w < kThreads / 32; ++w) t = fmaxf(t, st.red[w][i & 3]);
+      for (int w = 0; w < NT / 32; ++w) t = fmaxf(t, st.red[w][i & 3]);
       st.K[i] = epl_terms_from_maxf(t, a.epl.niter);
     }
     __syncthreads();
@@ -125,12 +126,12 @@ __device__ __forceinline__ int small_div(int i, float inv) {
 // block, output row) with the row fastest, so the eight threads of a
 // 16-byte load phase read eight consecutive plane rows of one column block:
 // with pitch / 4 odd they fall into eight distinct bank groups.
-template <int KS, int CB>
+template <int KS, int CB, int NT>
 __device__ void lsq_pass_conv(const LsqImage& I, const float* sm, int c0, int nb, int i0,
                               float* __restrict__ Xout /* X[b][0] */) {
   const int units = I.CPn * I.ncbC * nb;
   const float* kern = sm + I.offK;
-  for (int u = threadIdx.x; u < units; u += kThreads) {
+  for (int u = threadIdx.x; u < units; u += NT) {
     const int rest = u / nb;
     const int il = u - rest * nb;
     const int slot = rest / I.ncbC;
@@ -160,14 +161,18 @@ __device__ void lsq_pass_conv(const LsqImage& I, const float* sm, int c0, int nb
   do {                                                                       \
     if constexpr (KSV <= 15) {                                               \
       if (I.CB == 20) {                                                      \
-        lsq_pass_conv<KSV, 20>(I, sm, c0, nb, i0, Xb);                       \
+        lsq_pass_conv<KSV, 20, NT>(I, sm, c0, nb, i0, Xb);                   \
         break;                                                               \
       }                                                                      \
     }                                                                        \
-    lsq_pass_conv<KSV, 16>(I, sm, c0, nb, i0, Xb);                           \
+    lsq_pass_conv<KSV, 16, NT>(I, sm, c0, nb, i0, Xb);                       \
   } while (0)
 
-__global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_constant__ LsqArgs a) {
+// NT = 512 (one CTA per SM, whole-image planes when they fit) or 256 (two
+// CTAs per SM on row bands: one CTA's channel evaluation overlaps the other's
+// correlation).
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) lsq_basis_kernel(const __grid_constant__ LsqArgs a) {
   extern __shared__ float4 smem_dyn[];
   float* sm = reinterpret_cast<float*>(smem_dyn);
   __shared__ LsqShared st;
@@ -178,7 +183,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
     for (int i = 2; i <= tid; ++i) f *= i;
     pref[tid] = (float)(1.0 / sqrt(pow(2.0, tid) * sqrt(3.14159265358979323846) * f));
   }
-  lsq_term_counts(a, st);
+  lsq_term_counts<NT>(a, st);
   float2* beta = a.beta + (size_t)blockIdx.x * a.beta_stride;
   const int total = a.bs * a.max_bands;
   for (int item = blockIdx.x; item < total; item += gridDim.x) {
@@ -196,8 +201,8 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
     const float inv_n = 1.f / (float)I.N;
     if (tid < a.d) st.x[tid] = a.x[(size_t)b * a.d + tid];
     // zero the planes (halo rows and columns stay zero), load the sub-kernels
-    for (int i = tid; i < I.offK / 4; i += kThreads) smem_dyn[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int i = tid; i < I.nplanes * I.KS * I.ksp; i += kThreads) sm[I.offK + i] = __ldg(I.kern + i);
+    for (int i = tid; i < I.offK / 4; i += NT) smem_dyn[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = tid; i < I.nplanes * I.KS * I.ksp; i += NT) sm[I.offK + i] = __ldg(I.kern + i);
     __syncthreads();
     const int K = st.K[im];
     const int* e = a.epl.col;
@@ -215,7 +220,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
       for (int pq = 0; pq < I.nplanes; ++pq) {
         const float4* gp = grid + ((size_t)pq * I.N + Ya) * I.N;
         float2* bp = beta + (size_t)pq * per_plane;
-        for (int i = tid; i < per_plane; i += kThreads) {
+        for (int i = tid; i < per_plane; i += NT) {
           const float4 xy = __ldg(gp + i);
           float ax, ay;
           epl_deflect(ec, st.tab, xy.x, xy.y, ax, ay);
@@ -246,11 +251,11 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
           if (ch.kind == 1 && pr.interp) {   // tabulated shapelet functions (interpolate=True)
             const float beta_s = lpget(st.x, pr.col[0], 1.f);
             const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
-            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * kThreads) {
+            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * NT) {
               float u[kEvalU], w[kEvalU];
 #pragma unroll
               for (int k = 0; k < kEvalU; ++k) {
-                const int i = min(i0 + k * kThreads, per_plane - 1);
+                const int i = min(i0 + k * NT, per_plane - 1);
                 float px, py;
                 if (src) {
                   const float2 bt = bp[i];
@@ -266,7 +271,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
               }
 #pragma unroll
               for (int k = 0; k < kEvalU; ++k) {
-                const int i = i0 + k * kThreads;
+                const int i = i0 + k * NT;
                 if (i < per_plane) {
                   float val = shp_tab_value(a.shp_tab, ch.n1, shp_lerp(u[k])) *
                               shp_tab_value(a.shp_tab, ch.n2, shp_lerp(w[k]));
@@ -279,11 +284,11 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
           } else if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
             const float ib = 1.f / lpget(st.x, pr.col[0], 1.f);
             const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
-            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * kThreads) {
+            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * NT) {
               float u[kEvalU], w[kEvalU];
 #pragma unroll
               for (int k = 0; k < kEvalU; ++k) {
-                const int i = min(i0 + k * kThreads, per_plane - 1);
+                const int i = min(i0 + k * NT, per_plane - 1);
                 float px, py;
                 if (src) {
                   const float2 bt = bp[i];
@@ -302,7 +307,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
               hermite_fn_n<kEvalU>(ch.n2, w, hw, pref);
 #pragma unroll
               for (int k = 0; k < kEvalU; ++k) {
-                const int i = i0 + k * kThreads;
+                const int i = i0 + k * NT;
                 if (i < per_plane) {
                   const float fac = expf(-(u[k] * u[k] + w[k] * w[k]) / 2.f);
                   float val = fac * hu[k] * hw[k];
@@ -316,11 +321,11 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
             const SerC sc = sersic_consts(lpget(st.x, pr.col[0], 1.f), lpget(st.x, pr.col[1], 1.f),
                                           lpget(st.x, pr.col[2], 0.f), lpget(st.x, pr.col[3], 0.f),
                                           lpget(st.x, pr.col[4], 0.f), lpget(st.x, pr.col[5], 0.f), 1.f);
-            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * kThreads) {
+            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * NT) {
               float px[kEvalU], py[kEvalU];
 #pragma unroll
               for (int k = 0; k < kEvalU; ++k) {
-                const int i = min(i0 + k * kThreads, per_plane - 1);
+                const int i = min(i0 + k * NT, per_plane - 1);
                 if (src) {
                   const float2 bt = bp[i];
                   px[k] = bt.x;
@@ -333,7 +338,7 @@ __global__ void __launch_bounds__(kThreads, 1) lsq_basis_kernel(const __grid_con
               }
 #pragma unroll
               for (int k = 0; k < kEvalU; ++k) {
-                const int i = i0 + k * kThreads;
+                const int i = i0 + k * NT;
                 if (i < per_plane) {
                   float val = sersic_light(sc, px[k], py[k]);
                   if (isnan(val)) val = 0.f;
@@ -701,7 +706,140 @@ __global__ void lsq_weights_kernel(const float* __restrict__ err, const float* _
   }
 }
 // ------------------------------------------------------------------ host side
-static int g_lsq_smem_set[kMaxDevices];   // basis kernel smem attribute set per device
+static int g_lsq_smem_set[kMaxDevices][2];   // basis kernel smem attribute set per device and variant
+
+// Shared-memory layout and launch shape of the basis kernel for one tuning:
+// ctas_per_sm = 1 (512 threads, up to the whole opt-in shared memory of a
+// CTA) or 2 (256 threads, half the SM's shared memory each); col_block = 16
+// or 20 columns per correlation unit, 0 for the planner's choice.
+int lsq_plan_layout(LsqPlan* L, const gl_plan* plan, int ctas_per_sm, int col_block) {
+  if (ctas_per_sm != 1 && ctas_per_sm != 2) {
+    set_error("least squares: %d basis CTAs per SM (1 or 2)", ctas_per_sm);
+    return GL_ERR_INVALID;
+  }
+  if (col_block != 0 && col_block != 16 && col_block != 20) {
+    set_error("least squares: column block %d (16 or 20)", col_block);
+    return GL_ERR_INVALID;
+  }
+  const int D = L->D;
+  const int nt = ctas_per_sm == 1 ? 512 : 256;
+  int dev_smem = 0, sm_smem = 0;
+  cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
+  cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, plan->device);
+  const int static_bytes = 8 * 1024;
+  // per CTA: 1 KB of every CTA's shared memory is reserved by the system
+  const int cta_smem = ctas_per_sm == 1 ? dev_smem : std::min(dev_smem, sm_smem / 2 - 1024);
+  int maxP = 0, maxXc = 0, smem = 0, max_bands = 0;
+  size_t beta_per_cta = 0;
+  LsqImage img[GL_MAX_IMAGES];
+  for (int i = 0; i < plan->n_images; ++i) {
+    const DevImage& F = plan->img[i];
+    LsqImage I = L->img[i];
+    I.N = F.N;
+    I.ss = F.ss;
+    I.nplanes = F.nplanes;
+    I.KS = F.KS;
+    I.ksp = F.ksp;
+    for (int k = 0; k < kMaxPlanes; ++k) {
+      I.d[k] = F.d[k];
+      I.padI[k] = F.padI[k];
+    }
+    I.pitch = 0;
+    I.xcstride = (F.N * F.N + 3) & ~3;   // 16-byte aligned channel rows (cp.async)
+    I.cpass = D;
+    int dmin = F.d[0], dmax = F.d[0];
+    for (int p = 1; p < F.ss; ++p) {
+      dmin = std::min(dmin, F.d[p]);
+      dmax = std::max(dmax, F.d[p]);
+    }
+    I.R0 = dmax;
+    // Layout: per channel slot, ss^2 parity planes of brows rows x pitch
+    // floats (image rows with a top/bottom halo of the sub-kernel, columns
+    // with a zero right halo), then the sub-kernels.  Prefer the whole image
+    // in one band with as many channels per pass as fit; among column blocks
+    // of 16 and 20 pick the one that keeps the most of the threads busy.
+    const int kern_floats = F.nplanes * F.KS * F.ksp;
+    const int avail = cta_smem - static_bytes - kern_floats * 4;
+    double best_score = -1.0;
+    for (int cb : {20, 16}) {
+      if (cb == 20 && F.KS > 15) continue;
+      if (col_block && cb != col_block) continue;
+      const int ncbC = (F.N + cb - 1) / cb;
+      const int segn = (cb + F.KS - 1 + 3) & ~3;
+      int pitch = std::max(F.N + F.KS - 1, (ncbC - 1) * cb + segn);
+      pitch = (pitch + 3) & ~3;
+      if ((pitch / 4) % 2 == 0) pitch += 4;
+      // band height: the whole image when one channel's planes fit
+      int bo = F.N;
+      while (bo >= 1 && F.nplanes * (bo + F.KS + dmax - dmin) * pitch * 4 > avail) --bo;
+      if (bo < 1) continue;
+      const int brows = bo + F.KS + dmax - dmin;
+      const int set_bytes = F.nplanes * brows * pitch * 4;
+      const int cp_max = std::max(1, std::min(std::min(avail / set_bytes, D), 4));
+      for (int cp = 1; cp <= cp_max; ++cp) {
+        const int units = cp * ncbC * bo;
+        const int rounds = (units + nt - 1) / nt;
+        const double util = (double)cp * bo * F.N / ((double)rounds * nt * cb);
+        const double halo = (double)bo / std::min(brows, F.N);   // rows evaluated per output row
+        const double score = util * std::min(1.0, halo) * (1.0 + 0.02 * cp);
+        if (score > best_score) {
+          best_score = score;
+          I.CB = cb;
+          I.ncbC = ncbC;
+          I.pitch = pitch;
+          I.Bo = bo;
+          I.brows = brows;
+          I.CPn = cp;
+        }
+      }
+    }
+    if (best_score < 0) {
+      set_error("least squares: image %d does not fit in shared memory", i);
+      return GL_ERR_UNSUPPORTED;
+    }
+    I.nbands = (F.N + I.Bo - 1) / I.Bo;
+    I.plane_floats = I.brows * I.pitch;
+    I.offK = I.CPn * F.nplanes * I.plane_floats;
+    I.smem_floats = I.offK + kern_floats;
+    // the per-pixel loops divide indices below 2^21 through float reciprocals
+    if ((long long)F.nplanes * std::min(I.brows, F.N) * F.N >= (1 << 21)) {
+      set_error("least squares: image %d too large (%d px)", i, F.N);
+      return GL_ERR_UNSUPPORTED;
+    }
+    const size_t beta_n = (size_t)F.nplanes * std::min(I.brows, F.N) * F.N;
+    if (beta_n > beta_per_cta) beta_per_cta = beta_n;
+    if (I.smem_floats * 4 > smem) smem = I.smem_floats * 4;
+    if (F.N * F.N > maxP) maxP = F.N * F.N;
+    if (I.xcstride > maxXc) maxXc = I.xcstride;
+    if (I.nbands > max_bands) max_bands = I.nbands;
+    img[i] = I;
+  }
+  const int dev_slot = current_device_slot();
+  int* set = ctas_per_sm == 1 ? g_lsq_smem_set[dev_slot] + 0 : g_lsq_smem_set[dev_slot] + 1;
+  if (smem > *set) {
+    cudaError_t e = ctas_per_sm == 1
+                        ? cudaFuncSetAttribute(lsq_basis_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+                        : cudaFuncSetAttribute(lsq_basis_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) {
+      set_error("lsq smem attribute: %s", cudaGetErrorString(e));
+      return GL_ERR_CUDA;
+    }
+    *set = smem;
+  }
+  for (int i = 0; i < plan->n_images; ++i) L->img[i] = img[i];
+  L->smem_bytes = smem;
+  L->maxP = maxP;
+  L->maxXc = maxXc;
+  L->max_bands = max_bands;
+  L->beta_per_cta = beta_per_cta;
+  L->nt = nt;
+  L->ctas_per_sm = ctas_per_sm;
+  L->col_block = col_block;
+  int sms = 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
+  L->n_sm = ctas_per_sm * sms;
+  return GL_OK;
+}
 
 int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
   LsqPlan* L = new LsqPlan;
@@ -794,103 +932,20 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
     return GL_ERR_UNSUPPORTED;
   }
   L->D = D;
-  int dev_smem = 0;
-  cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
-  const int static_bytes = 8 * 1024;
-  int maxP = 0, maxXc = 0, smem = 0, max_bands = 0;
-  size_t beta_per_cta = 0;
   for (int i = 0; i < plan->n_images; ++i) {
     const DevImage& F = plan->img[i];
     LsqImage& I = L->img[i];
-    I.N = F.N;
-    I.ss = F.ss;
-    I.nplanes = F.nplanes;
-    I.KS = F.KS;
-    I.ksp = F.ksp;
-    for (int k = 0; k < kMaxPlanes; ++k) {
-      I.d[k] = F.d[k];
-      I.padI[k] = F.padI[k];
-    }
-    I.pitch = 0;
     I.grid = F.grid;
     I.kern = F.kern;
     I.obs = F.obs;
-    I.xcstride = (F.N * F.N + 3) & ~3;   // 16-byte aligned channel rows (cp.async)
-    I.cpass = D;
-    int dmin = F.d[0], dmax = F.d[0];
-    for (int p = 1; p < F.ss; ++p) {
-      dmin = std::min(dmin, F.d[p]);
-      dmax = std::max(dmax, F.d[p]);
-    }
-    I.R0 = dmax;
-    // Layout: per channel slot, ss^2 parity planes of brows rows x pitch
-    // floats (image rows with a top/bottom halo of the sub-kernel, columns
-    // with a zero right halo), then the sub-kernels.  Prefer the whole image
-    // in one band with as many channels per pass as fit; among column blocks
-    // of 16 and 20 pick the one that keeps the most of the 512 threads busy.
-    const int kern_floats = F.nplanes * F.KS * F.ksp;
-    const int avail = dev_smem - static_bytes - kern_floats * 4;
-    double best_score = -1.0;
-    for (int cb : {20, 16}) {
-      if (cb == 20 && F.KS > 15) continue;
-      const int ncbC = (F.N + cb - 1) / cb;
-      const int segn = (cb + F.KS - 1 + 3) & ~3;
-      int pitch = std::max(F.N + F.KS - 1, (ncbC - 1) * cb + segn);
-      pitch = (pitch + 3) & ~3;
-      if ((pitch / 4) % 2 == 0) pitch += 4;
-      // band height: the whole image when one channel's planes fit
-      int bo = F.N;
-      while (bo >= 1 && F.nplanes * (bo + F.KS + dmax - dmin) * pitch * 4 > avail) --bo;
-      if (bo < 1) continue;
-      const int brows = bo + F.KS + dmax - dmin;
-      const int set_bytes = F.nplanes * brows * pitch * 4;
-      const int cp_max = std::max(1, std::min(std::min(avail / set_bytes, D), 4));
-      for (int cp = 1; cp <= cp_max; ++cp) {
-        const int units = cp * ncbC * bo;
-        const int rounds = (units + kThreads - 1) / kThreads;
-        const double util = (double)cp * bo * F.N / ((double)rounds * kThreads * cb);
-        const double halo = (double)bo / std::min(brows, F.N);   // rows evaluated per output row
-        const double score = util * std::min(1.0, halo) * (1.0 + 0.02 * cp);
-        if (score > best_score) {
-          best_score = score;
-          I.CB = cb;
-          I.ncbC = ncbC;
-          I.pitch = pitch;
-          I.Bo = bo;
-          I.brows = brows;
-          I.CPn = cp;
-        }
-      }
-    }
-    if (best_score < 0) {
-      set_error("least squares: image %d does not fit in shared memory", i);
-      delete L;
-      return GL_ERR_UNSUPPORTED;
-    }
-    I.nbands = (F.N + I.Bo - 1) / I.Bo;
-    I.plane_floats = I.brows * I.pitch;
-    I.offK = I.CPn * F.nplanes * I.plane_floats;
-    I.smem_floats = I.offK + kern_floats;
-    // the per-pixel loops divide indices below 2^21 through float reciprocals
-    if ((long long)F.nplanes * std::min(I.brows, F.N) * F.N >= (1 << 21)) {
-      set_error("least squares: image %d too large (%d px)", i, F.N);
-      delete L;
-      return GL_ERR_UNSUPPORTED;
-    }
-    const size_t beta_n = (size_t)F.nplanes * std::min(I.brows, F.N) * F.N;
-    if (beta_n > beta_per_cta) beta_per_cta = beta_n;
-    if (I.smem_floats * 4 > smem) smem = I.smem_floats * 4;
-    if (F.N * F.N > maxP) maxP = F.N * F.N;
-    if (I.xcstride > maxXc) maxXc = I.xcstride;
-    if (I.nbands > max_bands) max_bands = I.nbands;
   }
-  L->smem_bytes = smem;
-  L->maxP = maxP;
-  L->maxXc = maxXc;
-  L->max_bands = max_bands;
-  L->beta_per_cta = beta_per_cta;
-  L->n_sm = 1;
-  cudaDeviceGetAttribute(&L->n_sm, cudaDevAttrMultiProcessorCount, plan->device);
+  {
+    int rc = lsq_plan_layout(L, plan, 1, 0);
+    if (rc) {
+      delete L;
+      return rc;
+    }
+  }
   // error maps, W = 1/err and b = W * obs on the device (W and b zero-padded
   // to whole streaming chunks)
   auto up256 = [](size_t v) { return (v + 255) / 256 * 256; };
@@ -932,17 +987,6 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
     cudaFree(L->dev_err);
     delete L;
     return GL_ERR_CUDA;
-  }
-  const int dev_slot = current_device_slot();
-  if (smem > g_lsq_smem_set[dev_slot]) {
-    cudaError_t e = cudaFuncSetAttribute(lsq_basis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) {
-      set_error("lsq smem attribute: %s", cudaGetErrorString(e));
-      cudaFree(L->dev_err);
-      delete L;
-      return GL_ERR_CUDA;
-    }
-    g_lsq_smem_set[dev_slot] = smem;
   }
   plan->lsq = L;
   return GL_OK;
@@ -1035,7 +1079,10 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
   cudaMemsetAsync(status, 0, sizeof(int), stream);
   // basis stack, then G = A^T A and h = A^T b on the tensor cores (3xTF32)
-  lsq_basis_kernel<<<n_basis, kThreads, L->smem_bytes, stream>>>(a);
+  if (L->nt == 512)
+    lsq_basis_kernel<512><<<n_basis, 512, L->smem_bytes, stream>>>(a);
+  else
+    lsq_basis_kernel<256><<<n_basis, 256, L->smem_bytes, stream>>>(a);
   const int gram_grid = std::min(bs, gram_tc_ctas_per_sm(L->D) * sms);
   int rc = launch_gram_tc(a, G, h, status, gram_grid, stream);
   if (rc) return rc;
@@ -1166,4 +1213,48 @@ extern "C" int gl_lstsq_noalloc(const gl_plan* plan, const float* x, const int* 
   if (rc) return rc;
   return lsq_run(plan, x, img_id, bs, (float*)scratch, kNoAllocScratchBytes, coeffs, img_out, logL,
                  chi2, (cudaStream_t)stream);
+}
+
+
+extern "C" int gl_plan_set_tuning(gl_plan* plan, const gl_tuning* t) {
+  using namespace gl;
+  if (!plan || !t) {
+    set_error("gl_plan_set_tuning: null plan or tuning");
+    return GL_ERR_INVALID;
+  }
+  if (t->fused_corr < 0 || t->fused_corr > 2) {
+    set_error("gl_plan_set_tuning: fused_corr %d (1 FFMA2, 2 scalar FFMA)", t->fused_corr);
+    return GL_ERR_INVALID;
+  }
+  if (t->fused_corr) plan->corr_scalar = t->fused_corr == 2;
+  if (!plan->lsq || (t->lsq_ctas_per_sm == 0 && t->lsq_col_block == 0)) return GL_OK;
+  LsqPlan* L = (LsqPlan*)plan->lsq;
+  const int ctas = t->lsq_ctas_per_sm ? t->lsq_ctas_per_sm : L->ctas_per_sm;
+  const int cb = t->lsq_col_block == 0 ? L->col_block : (t->lsq_col_block < 0 ? 0 : t->lsq_col_block);
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != plan->device) {
+    set_error("plan was created on device %d but device %d is current", plan->device, dev);
+    return GL_ERR_INVALID;
+  }
+  LsqPlan saved = *L;
+  int rc = lsq_plan_layout(L, plan, ctas, cb);
+  if (rc) *L = saved;   // keep the previous, valid layout
+  return rc;
+}
+
+extern "C" int gl_plan_get_tuning(const gl_plan* plan, gl_tuning* t) {
+  using namespace gl;
+  if (!plan || !t) {
+    set_error("gl_plan_get_tuning: null plan or tuning");
+    return GL_ERR_INVALID;
+  }
+  memset(t, 0, sizeof(*t));
+  t->fused_corr = plan->corr_scalar ? 2 : 1;
+  if (plan->lsq) {
+    const LsqPlan* L = (const LsqPlan*)plan->lsq;
+    t->lsq_ctas_per_sm = L->ctas_per_sm;
+    t->lsq_col_block = L->img[0].CB;
+  }
+  return GL_OK;
 }

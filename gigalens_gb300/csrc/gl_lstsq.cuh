@@ -67,7 +67,9 @@ struct LsqArgs {
 struct LsqPlan {
   int D, n_prof, has_shear, maxP, max_bands, smem_bytes;
   int maxXc;            // largest per-channel stride of X (floats)
-  int n_sm;             // CTAs of the basis kernel at most (one per SM)
+  int n_sm;             // CTAs of the basis kernel at most (ctas_per_sm per SM)
+  int nt, ctas_per_sm;  // basis kernel: threads per CTA (512 or 256) and CTAs per SM
+  int col_block;        // forced correlation column block (0: planner's choice)
   size_t beta_per_cta;  // float2 of the largest band's ray-traced coordinates
   LsqProfile prof[kMaxLsqProfiles];
   LsqChannel ch[kMaxLsqChannels];
@@ -77,6 +79,7 @@ struct LsqPlan {
 };
 
 int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs);
+int lsq_plan_layout(LsqPlan* L, const gl_plan* plan, int ctas_per_sm, int col_block);
 // tensor-core Gram (gl_gram_tc.cu)
 int launch_gram_tc(const LsqArgs& a, float* G, float* h, int* status, int grid, cudaStream_t stream);
 int gram_tc_smem_bytes(int D);

@@ -86,6 +86,12 @@ class ModelLayout:
         self.desc = desc
         self.d = desc.n_params
 
+    def signature(self) -> str:
+        """Profile types, groups and orders, e.g. for keying tuned launch shapes."""
+        d = self.desc
+        return ";".join("%d.%d.%d.%d.%d" % (d.prof[i].type, d.prof[i].group, d.prof[i].niter, d.prof[i].use_lstsq,
+                                           d.prof[i].interpolate) for i in range(d.n_profiles))
+
     def split(self, params):
         """``(lens, lens_light, source)`` lists from a reference-style structure
         (``tf/simulator.py:67-72``)."""

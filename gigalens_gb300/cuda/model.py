@@ -11,6 +11,7 @@ import numpy as np
 import torch
 
 from .. import _native as N
+from . import autotune
 from .. import distributions as dist
 from .. import model as _model
 
@@ -38,7 +39,9 @@ class _LogProb(torch.autograd.Function):
 
 
 def log_prob_and_grad(plan, z, logp=None, chi2=None, grad=None, img_id=None, stream=None):
-    """Fused ``logp, chi2, d logp / dz`` into caller buffers (graph-capturable)."""
+    """Fused ``logp, chi2, d logp / dz`` into caller buffers (graph-capturable;
+    the plan's launch shape is tuned on the first call outside a capture)."""
+    autotune.ensure_fused(plan, z, img_id)
     bs = z.shape[0]
     N.call("gl_log_prob", plan.handle, N.ptr(z), N.ptr(img_id), bs, N.ptr(logp), N.ptr(chi2), N.ptr(grad),
            None, N.stream_ptr(stream))
@@ -70,6 +73,7 @@ class ForwardProbModel(_model.ProbabilisticModel):
             z = z.to(torch.device("cuda", torch.cuda.current_device()))
         if z.dim() == 1:
             z = z[None]
+        autotune.ensure_fused(plan, z.detach().to(torch.float32).contiguous())
         return _LogProb.apply(z, plan, None)
 
 

@@ -12,6 +12,7 @@ import numpy as np
 import torch
 
 from .. import _native as N
+from . import autotune
 from .. import simulator as _sim
 from ._plan import ModelLayout, Plan
 
@@ -86,6 +87,7 @@ class LensSimulator(_sim.LensSimulatorInterface):
         """Run the least-squares kernels on flat physical parameters ``x``."""
         x = x.to(torch.float32).contiguous()
         bs = x.shape[0]
+        autotune.ensure_lstsq(plan, x)   # before the workspace query: the tuning sets its size
         nbytes = ctypes.c_size_t(0)
         D = ctypes.c_int(0)
         N.call("gl_lstsq_workspace", plan.handle, bs, ctypes.byref(nbytes), ctypes.byref(D))

@@ -146,7 +146,7 @@ typedef struct gl_plan gl_plan;
 int gl_abi_version(void);
 /* sizeof of the public structs, for bindings to check their mirrors:
  * 0 gl_profile_desc, 1 gl_model_desc, 2 gl_image_desc, 3 gl_prior_leaf,
- * 4 gl_tune_result, 5 gl_adam_cfg; -1 for any other index.               */
+ * 4 gl_tune_result, 5 gl_adam_cfg, 6 gl_tuning; -1 for any other index.  */
 int gl_struct_size(int which);
 const char* gl_last_error(void);
 /* Number of SMs and the opt-in shared memory per block of the current device. */
@@ -268,12 +268,15 @@ int gl_lstsq_status(const gl_plan* plan, int bs, const void* work, int* status, 
  * once.  Not for production use.                                          */
 int gl_test_set_wait_polls(int polls);
 
-/* Launch configuration of the fused kernel for a batch of bs samples.  The
- * correlation tile (16 outputs per lane, quarter-warp groups of 4 rows x 2
- * blocks), the block size (512 threads, 16 warps) and the interleave depth
- * are fixed at compile time for sm_103a; the grid is persistent (one CTA per
- * SM, at most bs), so there is nothing to search and the result is the
- * configuration the plan's launches use.                                   */
+/* Launch configuration of the fused kernel for a batch of bs samples
+ * (no reference counterpart: TensorFlow/XLA choose the reference's kernels).
+ * The correlation tile (16 outputs per lane, quarter-warp groups of 4 rows x
+ * 2 blocks), the block size (512 threads, 16 warps) and the interleave depth
+ * are compiled for sm_103a and the grid is persistent (one CTA per SM, at
+ * most bs); the least-squares basis kernel's shape is the plan's tuning
+ * (gl_plan_set_tuning, chosen by timing in gigalens_gb300.cuda.autotune and
+ * cached per plan shape).  The result is the configuration the plan's
+ * launches use.                                                            */
 typedef struct {
   int threads_per_block;
   int blocks;              /* CTAs of a launch of bs samples            */
@@ -285,6 +288,31 @@ typedef struct {
   int col_block;           /* correlation outputs per lane              */
 } gl_tune_result;
 int gl_autotune(const gl_plan* plan, int bs, gl_tune_result* out);
+
+/* Tunable launch shape of a plan (no reference counterpart).  The timing
+ * search over these values lives on the host side (cuda/autotune.py): it
+ * times each candidate on the caller's inputs, keeps the fastest and caches
+ * it per plan shape.  Changing the least-squares fields re-plans the basis
+ * kernel's shared-memory layout, which changes gl_lstsq_workspace(): query
+ * it again afterwards.  Fields left 0 keep the current value.
+ *   lsq_ctas_per_sm  1: 512 threads per CTA, whole-image parity planes when
+ *                    they fit; 2: two CTAs of 256 threads per SM on row bands,
+ *                    so one CTA's channel evaluation overlaps the other's
+ *                    correlation
+ *   lsq_col_block    output columns per correlation unit: 16 or 20, or -1
+ *                    for the planner's choice
+ *   fused_corr       the fused kernel's PSF correlations (EPL + shear +
+ *                    Sersic lens light + Sersic source, image planes in
+ *                    shared memory): 1 packed FFMA2, 2 scalar FFMA; other
+ *                    models always use FFMA2                              */
+typedef struct {
+  int lsq_ctas_per_sm;
+  int lsq_col_block;
+  int fused_corr;
+  int reserved[5];
+} gl_tuning;
+int gl_plan_set_tuning(gl_plan* plan, const gl_tuning* t);
+int gl_plan_get_tuning(const gl_plan* plan, gl_tuning* t);
 
 /* Gradient of the BackwardProbModel likelihood (tf/model.py:152-158: the
  * least-squares image scored with the data-based error map) with respect to

@@ -46,7 +46,7 @@ def test_struct_mirrors_match_the_header():
     """The ctypes mirrors have the C structs' sizes (a field added on one side
     only would shift every later field)."""
     mirrors = [N.gl_profile_desc, N.gl_model_desc, N.gl_image_desc, N.gl_prior_leaf, N.gl_tune_result,
-               N.gl_adam_cfg]
+               N.gl_adam_cfg, N.gl_tuning]
     lib = N.lib()
     for i, m in enumerate(mirrors):
         assert lib.gl_struct_size(i) == ctypes.sizeof(m), (m.__name__, lib.gl_struct_size(i), ctypes.sizeof(m))

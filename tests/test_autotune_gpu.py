@@ -1,0 +1,152 @@
+"""Launch-shape autotuner (gigalens_gb300.cuda.autotune): the timing search
+runs once per plan shape, a second plan of the same shape takes the cached
+choice without timing, every candidate computes the same results, and the
+tuned shape is not slower than the default one on the bench workloads."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from gigalens_gb300 import _native as N
+from gigalens_gb300 import workloads as W
+from gigalens_gb300.cuda import autotune
+from gigalens_gb300.cuda.model import ForwardProbModel
+from gigalens_gb300.cuda.simulator import LensSimulator
+
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+
+@pytest.fixture()
+def fresh_cache(tmp_path, monkeypatch):
+    monkeypatch.setenv("GIGALENS_GB300_TUNING", str(tmp_path / "tuning.json"))
+    monkeypatch.setenv("GIGALENS_GB300_AUTOTUNE", "1")
+    autotune.clear_memory_cache()
+    yield tmp_path / "tuning.json"
+    autotune.clear_memory_cache()
+
+
+def _fused_setup(bs, n_pix=60, psf_base=11):
+    phys = W.physical_model()
+    cfg = W.sim_config(n_pix, psf_base)
+    truth = LensSimulator(phys, cfg, bs=1).simulate(W.draw_params(1, seed=0)).cpu().numpy()
+    obs = np.random.default_rng(5).normal(truth, 0.2).astype(np.float32)
+    pm = ForwardProbModel(W.config_prior(), obs, background_rms=W.BG_RMS, exp_time=W.EXP_TIME)
+    sim = LensSimulator(phys, cfg, bs=bs)
+    z = pm.bij.inverse(W.draw_params(bs, seed=2)).to(torch.float32).cuda().contiguous()
+    return pm, sim, z
+
+
+def _log_prob(plan, z):
+    bs = z.shape[0]
+    logp, chi2, grad = torch.empty(bs, device="cuda"), torch.empty(bs, device="cuda"), torch.empty_like(z)
+    N.call("gl_log_prob", plan.handle, N.ptr(z), None, bs, N.ptr(logp), N.ptr(chi2), N.ptr(grad), None,
+           N.stream_ptr())
+    torch.cuda.synchronize()
+    return logp, grad
+
+
+def test_fused_choice_is_cached_and_reused(fresh_cache):
+    pm, sim, z = _fused_setup(64)
+    t0, c0 = autotune.stats["timed"], autotune.stats["cached"]
+    pm.log_prob(sim, z)                       # first call: times both variants
+    assert autotune.stats["timed"] == t0 + 1
+    choice = autotune.get_tuning(sim.prob_plan(pm))
+    assert fresh_cache.exists()
+    # a second simulator (second plan) of the same shape: cached, not timed
+    sim2 = LensSimulator(W.physical_model(), W.sim_config(60, 11), bs=64)
+    pm.log_prob(sim2, z)
+    assert autotune.stats["timed"] == t0 + 1 and autotune.stats["cached"] == c0 + 1
+    assert autotune.get_tuning(sim2.prob_plan(pm))["fused_corr"] == choice["fused_corr"]
+    # and the next process reads it from the file
+    autotune.clear_memory_cache()
+    sim3 = LensSimulator(W.physical_model(), W.sim_config(60, 11), bs=64)
+    pm.log_prob(sim3, z)
+    assert autotune.stats["timed"] == t0 + 1 and autotune.stats["cached"] == c0 + 2
+
+
+def test_fused_variants_agree(fresh_cache):
+    pm, sim, z = _fused_setup(32)
+    plan = sim.prob_plan(pm)
+    out = []
+    for corr in (1, 2):
+        autotune.set_tuning(plan, fused_corr=corr)
+        out.append(_log_prob(plan, z))
+    (l1, g1), (l2, g2) = out
+    assert float(((l1 - l2).abs() / l2.abs().clamp_min(1.0)).max()) < 1e-5
+    assert float(((g1 - g2).abs().amax(1) / g2.abs().amax(1)).max()) < 1e-4
+
+
+def test_lstsq_choice_is_cached_and_variants_agree(fresh_cache):
+    import bench
+    t0, c0 = autotune.stats["timed"], autotune.stats["cached"]
+    lsq = bench.lstsq_workload(torch, torch.device("cuda"), 96, 32)[0]   # tuned on first use
+    assert autotune.stats["timed"] == t0 + 1
+    lsq2 = bench.lstsq_workload(torch, torch.device("cuda"), 96, 32)[0]  # second plan, same shape
+    assert autotune.stats["timed"] == t0 + 1 and autotune.stats["cached"] == c0 + 1
+    assert lsq2.tuning == lsq.tuning
+    # every candidate gives the same coefficients and likelihoods (to rounding)
+    plan = lsq.plan
+    x, img_id = lsq.inputs
+    bs = x.shape[0]
+    res = []
+    for ctas in (1, 2):
+        for cb in (16, 20):
+            autotune.set_tuning(plan, lsq_ctas_per_sm=ctas, lsq_col_block=cb)
+            nb, D = ctypes.c_size_t(0), ctypes.c_int(0)
+            N.call("gl_lstsq_workspace", plan.handle, bs, ctypes.byref(nb), ctypes.byref(D))
+            work = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+            co, lg = torch.empty(bs, D.value, device="cuda"), torch.empty(bs, device="cuda")
+            N.call("gl_lstsq", plan.handle, N.ptr(x), N.ptr(img_id), bs, N.ptr(work), nb.value, N.ptr(co), None,
+                   N.ptr(lg), None, N.stream_ptr())
+            torch.cuda.synchronize()
+            res.append((co, lg))
+    for co, lg in res[1:]:
+        assert float(((lg - res[0][1]).abs() / res[0][1].abs()).max()) < 1e-5
+        scale = res[0][0].abs().amax(1, keepdim=True)
+        assert float(((co - res[0][0]).abs() / scale).max()) < 1e-3
+
+
+def _median_ms(fn, reps=7):
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    return sorted(ts)[reps // 2]
+
+
+def test_tuned_not_slower_than_default_on_bench_shapes(fresh_cache):
+    # headline: 4096 chains x 90^2, 41-pixel supersampled PSF
+    phys = W.physical_model()
+    cfg = W.config1()
+    truth = LensSimulator(phys, cfg, bs=1).simulate(W.draw_params(1, seed=0)).cpu().numpy()
+    obs = np.random.default_rng(5).normal(truth, 0.2).astype(np.float32)
+    pm = ForwardProbModel(W.config_prior(), obs, background_rms=W.BG_RMS, exp_time=W.EXP_TIME)
+    sim = LensSimulator(phys, cfg, bs=4096)
+    z = pm.bij.inverse(W.draw_params(4096, seed=1)).to(torch.float32).cuda().contiguous()
+    plan = sim.prob_plan(pm)
+    autotune.ensure_fused(plan, z)
+    tuned = autotune.get_tuning(plan)
+    t_tuned = _median_ms(lambda: _log_prob(plan, z))
+    autotune.set_tuning(plan, fused_corr=1)   # the default
+    t_default = _median_ms(lambda: _log_prob(plan, z))
+    print("\n[autotune] fused 4096x90^2: tuned %s %.3f ms, default %.3f ms" % (tuned, t_tuned, t_default))
+    assert t_tuned <= 1.02 * t_default
+    # least squares: 2048 x 100^2 + 512 x 60^2, n_max = 8
+    import bench
+    lsq = bench.lstsq_workload(torch, torch.device("cuda"), 2048, 512)[0]
+    t_tuned = _median_ms(lsq, reps=5)
+    tuned = lsq.tuning
+    lsq_d = bench.lstsq_workload(torch, torch.device("cuda"), 2048, 512, tuning=(1, -1))[0]
+    t_default = _median_ms(lsq_d, reps=5)
+    print("[autotune] lstsq 2048x100^2+512x60^2: tuned %s %.3f ms, default %.3f ms" % (tuned, t_tuned, t_default))
+    assert t_tuned <= 1.02 * t_default
