@@ -236,6 +236,10 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
         p0 = torch.empty_like(z)
         pp = torch.empty_like(z)
         u_acc = torch.empty(n_hmc, device=dev)
+        z_before = torch.empty_like(z)
+        log_acc = torch.empty(n_hmc, device=dev)
+        it_dev = torch.zeros(1, dtype=torch.int64, device=dev)   # iteration index (trace slot)
+        L_host = torch.empty(1, dtype=torch.int32).pin_memory()
         eps_dev = da.step_size                  # (1,) device tensor
 
         def kinetic(p):
@@ -259,61 +263,85 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
             z.copy_(torch.where(accept[:, None], zp, z))
             g.copy_(torch.where(accept[:, None], gp, g))
             logp.copy_(torch.where(accept, lpp, logp))
-            return log_accept
+            log_acc.copy_(log_accept)
+
+        # Per iteration: `pre` (the trajectory length on the device), the
+        # leapfrog transition of that length, `post` (traces and adaptation on
+        # the device).  With use_graph each piece is a CUDA graph, one per
+        # leapfrog count; the host reads only the count (one 4-byte copy) to
+        # pick the graph.  A piece runs eagerly the first time and is captured
+        # afterwards, so graph and eager runs execute the same kernels with the
+        # same random numbers.
+        def pre(adapting):
+            if chees is None:
+                return None
+
+            def f():
+                if adapting:
+                    z_before.copy_(z)
+                    chees.draw_steps(eps_dev)
+                else:
+                    chees.final_steps(eps_dev)
+            return f
+
+        def post(adapting, at_end):
+            def f():
+                acc_trace.index_copy_(0, it_dev, torch.exp(torch.clamp(log_acc, max=0.0)).mean().reshape(1))
+                if adapt_step_size and adapting:
+                    da.update(log_acc)
+                elif adapt_step_size and at_end:
+                    da.finalize()
+                if chees is not None and adapting:
+                    chees.update(z_before, z, pp @ cov, log_acc, eps_dev)
+                eps_trace.index_copy_(0, it_dev, eps_dev)
+                it_dev.add_(1)
+            return f
 
         graphs = {}
+
+        def run(key, fn):
+            if fn is None:
+                return
+            if not use_graph:
+                fn()
+                return
+            gph = graphs.get(key)
+            if gph is None:
+                fn()                            # this iteration's real work
+                graphs[key] = _capture_only(fn)
+            else:
+                gph.replay()
+
         for it in range(total):
             adapting = it < n_adapt
-            if chees is not None and adapting:
-                L = chees.draw_steps(float(eps_dev), gen)
-            elif chees is not None:
-                L = chees.final_steps(float(eps_dev))
+            run(("pre", adapting), pre(adapting))
+            if chees is not None:
+                L_host.copy_(chees.L_dev, non_blocking=False)
+                L = int(L_host[0])
             else:
                 L = int(init_l)
             L_trace.append(L)
-            z_before = z.clone() if (chees is not None and adapting) else None
-            if use_graph and not (chees is not None and adapting):
-                gph = graphs.get(L)
-                if gph is None:
-                    gph = _capture(lambda: leapfrog(L))
-                    graphs[L] = gph
-                gph.graph.replay()
-                log_accept = gph.out
-            else:
-                log_accept = leapfrog(L)
-            acc = torch.exp(torch.clamp(log_accept, max=0.0)).mean()
-            acc_trace[it] = acc
-            if adapt_step_size and adapting:
-                da.update(log_accept)
-            elif adapt_step_size and it == n_adapt:
-                da.finalize()
-            if z_before is not None:
-                chees.update(z_before, z, pp @ cov, log_accept, L, float(eps_dev))
-            eps_trace[it] = eps_dev[0]
+            run(("leap", L), lambda: leapfrog(L))
+            run(("post", adapting, it == n_adapt), post(adapting, it == n_adapt))
             if it >= num_burnin_steps:
                 samples[it - num_burnin_steps].copy_(z)
         stats = {"accept_ratio": acc_trace, "step_size": eps_trace,
-                 "leapfrog_steps": torch.tensor(L_trace), "target_log_prob": logp}
+                 "leapfrog_steps": torch.tensor(L_trace), "target_log_prob": logp,
+                 "graphs": len(graphs)}
         return samples, stats
 
 
-class _Captured:
-    def __init__(self, graph, out):
-        self.graph = graph
-        self.out = out
-
-
-def _capture(fn):
-    """Warm up ``fn`` once on a side stream, then capture it in a CUDA graph."""
+def _capture_only(fn):
+    """Capture ``fn`` in a CUDA graph without running it (the caller has just
+    run it eagerly, which also warmed up the libraries it calls)."""
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(s):
-        fn()
-    torch.cuda.current_stream().wait_stream(s)
     g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
-        out = fn()
-    return _Captured(g, out)
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            fn()
+    torch.cuda.current_stream().wait_stream(s)
+    return g
 
 
 def _run_steps(step, num_steps, use_graph):
@@ -380,11 +408,11 @@ class _DualAveraging:
         self.target, self.gamma, self.t0, self.kappa = target, shrinkage, t0, kappa
         self.err_sum = torch.zeros(1, device=dev)
         self.log_avg = torch.tensor([math.log(init_eps)], device=dev)
-        self.t = 0
+        self.t = torch.zeros(1, device=dev)   # updates so far (on the device: graph-replayable)
 
     def update(self, log_accept):
-        self.t += 1
-        t = float(self.t)
+        self.t.add_(1.0)
+        t = self.t
         la = torch.clamp(log_accept, max=0.0)
         if self.reduce == "mean":
             p = torch.exp(la).mean()
@@ -392,10 +420,10 @@ class _DualAveraging:
             # log-harmonic-mean-exp of the acceptance ratios over chains
             red = -(torch.logsumexp(-la, 0) - math.log(la.numel()))
             p = torch.exp(red)
-        self.err_sum += self.target - p
-        log_eps = self.mu - math.sqrt(t) / self.gamma * self.err_sum / (t + self.t0)
-        w = t ** (-self.kappa)
-        self.log_avg = w * log_eps + (1 - w) * self.log_avg
+        self.err_sum.add_(self.target - p)
+        log_eps = self.mu - torch.sqrt(t) / self.gamma * self.err_sum / (t + self.t0)
+        w = torch.pow(t, -self.kappa)
+        self.log_avg.copy_(w * log_eps + (1 - w) * self.log_avg)
         self.step_size.copy_(torch.exp(log_eps))
 
     def finalize(self):
@@ -404,36 +432,49 @@ class _DualAveraging:
 
 class _ChEES:
     """Trajectory length adaptation by the ChEES criterion (jittered lengths,
-    Adam on log T with learning rate 0.025, beta1 = 0)."""
+    Adam on log T with learning rate 0.025, beta1 = 0).  All state lives on
+    the device, so the adapting iterations replay as CUDA graphs; the
+    leapfrog count of the next transition is ``L_dev``."""
 
     def __init__(self, init_T, max_steps, dev, lr=0.025, beta2=0.95):
-        self.logT = math.log(max(init_T, 1e-6))
         self.max_steps = int(max_steps)
-        self.lr, self.b2, self.v, self.k = lr, beta2, 0.0, 0
-        self.avg_logT = self.logT
-        self.u = 1.0
+        self.lr, self.b2 = lr, beta2
+        self.logT = torch.tensor([math.log(max(init_T, 1e-6))], device=dev)
+        self.avg_logT = self.logT.clone()
+        self.v = torch.zeros(1, device=dev)
+        self.k = torch.zeros(1, device=dev)
+        self.u = torch.ones(1, device=dev)
+        self.L_dev = torch.ones(1, dtype=torch.int32, device=dev)
 
-    def draw_steps(self, eps, gen):
-        self.u = float(torch.rand(1, generator=gen, device=gen.device)) * 0.999 + 0.001
-        T = math.exp(self.logT) * self.u
-        return int(min(self.max_steps, max(1, math.ceil(T / max(eps, 1e-12)))))
+    def _steps(self, T, eps):
+        L = torch.ceil(T / torch.clamp(eps, min=1e-12))
+        self.L_dev.copy_(torch.clamp(torch.nan_to_num(L, nan=1.0), 1.0, float(self.max_steps)).to(torch.int32))
+
+    def draw_steps(self, eps):
+        """Jitter u ~ U(0.001, 1) (the default CUDA generator) and L = ceil(u T / eps)."""
+        self.u.copy_(torch.rand(1, device=self.u.device) * 0.999 + 0.001)
+        self._steps(torch.exp(self.logT) * self.u, eps)
 
     def final_steps(self, eps):
-        return int(min(self.max_steps, max(1, math.ceil(math.exp(self.avg_logT) / max(eps, 1e-12)))))
+        self._steps(torch.exp(self.avg_logT), eps)
 
-    def update(self, z0, z1, v1, log_accept, L, eps):
+    def update(self, z0, z1, v1, log_accept, eps):
         a = torch.exp(torch.clamp(log_accept, max=0.0))
         m0 = z0.mean(0, keepdim=True)
         m1 = z1.mean(0, keepdim=True)
         diff = ((z1 - m1) ** 2).sum(1) - ((z0 - m0) ** 2).sum(1)
-        gT = float((a * diff * ((z1 - m1) * v1).sum(1)).sum() / a.sum().clamp_min(1e-12)) * self.u
-        g = -gT * math.exp(self.logT)          # gradient of -ChEES with respect to log T
-        if not math.isfinite(g):
-            return
-        self.k += 1
-        self.v = self.b2 * self.v + (1 - self.b2) * g * g
-        vhat = self.v / (1 - self.b2 ** self.k)
-        self.logT -= self.lr * g / (math.sqrt(vhat) + 1e-8)
-        self.logT = min(self.logT, math.log(self.max_steps * max(eps, 1e-12)))
-        w = self.k ** -0.75
-        self.avg_logT = w * self.logT + (1 - w) * self.avg_logT
+        gT = (a * diff * ((z1 - m1) * v1).sum(1)).sum() / a.sum().clamp_min(1e-12) * self.u
+        g = -gT * torch.exp(self.logT)          # gradient of -ChEES with respect to log T
+        ok = torch.isfinite(g)
+        g = torch.where(ok, g, torch.zeros_like(g))
+        k = self.k + ok.float()
+        v = torch.where(ok, self.b2 * self.v + (1 - self.b2) * g * g, self.v)
+        vhat = v / (1 - torch.pow(torch.full_like(k, self.b2), k)).clamp_min(1e-30)
+        logT = self.logT - self.lr * g / (torch.sqrt(vhat) + 1e-8)
+        logT = torch.minimum(logT, torch.log(self.max_steps * torch.clamp(eps, min=1e-12)))
+        w = torch.pow(k.clamp_min(1.0), -0.75)
+        avg = w * logT + (1 - w) * self.avg_logT
+        self.logT.copy_(torch.where(ok, logT, self.logT))
+        self.avg_logT.copy_(torch.where(ok, avg, self.avg_logT))
+        self.v.copy_(v)
+        self.k.copy_(k)

@@ -141,3 +141,26 @@ def test_hmc_chees_and_dual_averaging_match_target_when_likelihood_is_flat(defau
     assert ((flat.mean(0) - mean).abs() / sd).max() < 0.1
     assert ((flat.std(0) / sd) - 1).abs().max() < 0.1
     assert potential_scale_reduction(s.float()).max() < 1.05
+
+
+def test_hmc_chees_graph_equals_eager(default_prior, default_physmodel):
+    """The adaptive warm-up (ChEES trajectory lengths + dual-averaging step
+    size) replayed from CUDA graphs, one per leapfrog count, draws exactly
+    what the eager run draws for the same seed."""
+    from gigalens_gb300.cuda.inference import MultivariateNormalTriL
+
+    seq, pm = _seq(default_prior, default_physmodel, data=(np.zeros((20, 20)), 1e4, 100))
+    zs = pm.bij.inverse(default_prior.sample(4000, seed=6)).double()
+    mean, cov = zs.mean(0), torch.cov(zs.T)
+    q = MultivariateNormalTriL(mean.float().cuda(), torch.linalg.cholesky(cov).float().cuda())
+    runs = []
+    for use_graph in (False, True):
+        samples, stats = seq.HMC(q, init_eps=0.3, init_l=3, n_hmc=64, num_burnin_steps=40, num_results=12,
+                                 max_leapfrog_steps=12, seed=7, use_graph=use_graph)
+        runs.append((samples.cpu(), stats))
+    (s0, st0), (s1, st1) = runs
+    assert torch.equal(st0["leapfrog_steps"], st1["leapfrog_steps"])
+    assert len(set(st1["leapfrog_steps"][:32].tolist())) > 1          # the lengths really vary
+    assert st1["graphs"] > 3 and st0["graphs"] == 0
+    assert torch.equal(st0["step_size"].cpu(), st1["step_size"].cpu())
+    assert torch.equal(s0, s1)
