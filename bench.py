@@ -366,11 +366,12 @@ def run_sequence(args):
     best, _ = timed(seq.best)
     i_best = int(torch.argmax(torch.nan_to_num(seq.map_log_prob, nan=-float("inf"))))
     map_chi2_dof = float(seq.map_chi2[i_best])   # the likelihood's chi^2 is a mean over pixels
-    (q_z, losses), t_svi = timed(lambda: seq.SVI(Adam(PolynomialDecay(0.0, 500, 1e-3, 2)), best,
+    (q_z, losses), t_svi = timed(lambda: seq.SVI(Adam(PolynomialDecay(0.0, 500, args.seq_svi_lr, 2)), best,
                                                  n_vi=1024, num_steps=args.seq_svi_steps))
+    burnin = args.seq_hmc_burnin
     (samples, stats), t_hmc = timed(lambda: seq.HMC(q_z, init_eps=0.3, init_l=8, n_hmc=args.seq_hmc_chains,
-                                                    num_burnin_steps=500, num_results=args.seq_hmc_results,
-                                                    adapt_trajectory=False,
+                                                    num_burnin_steps=burnin, num_results=args.seq_hmc_results,
+                                                    adapt_trajectory=args.seq_adapt_trajectory,
                                                     step_size_reduce=args.seq_step_reduce))
     rhat = potential_scale_reduction(samples)
     ess = effective_sample_size(samples)
@@ -392,20 +393,24 @@ def run_sequence(args):
     plan1 = LensSimulator(phys, cfg, bs=1).prob_plan(pm)
     lp1, c21 = torch.empty(1, device=dev), torch.empty(1, device=dev)
     log_prob_and_grad(plan1, mean_z, lp1, c21, None)
-    line = {"metric": "modelling sequence wall time @90^2px (MAP %dx350 -> SVI 1024x%d -> HMC %dx(500+%d), L=8)"
-                      % (args.seq_map_chains, args.seq_svi_steps, args.seq_hmc_chains, args.seq_hmc_results),
+    Ls = stats["leapfrog_steps"]
+    line = {"metric": "modelling sequence wall time @90^2px (MAP %dx350 -> SVI 1024x%d -> HMC %dx(%d+%d), %s)"
+                      % (args.seq_map_chains, args.seq_svi_steps, args.seq_hmc_chains, burnin, args.seq_hmc_results,
+                         "ChEES trajectory lengths" if args.seq_adapt_trajectory else "L=8"),
             "value": t_map + t_svi + t_hmc, "unit": "s", "higher_is_better": False, "data": "synthetic",
             "stages_s": {"map": t_map, "svi": t_svi, "hmc": t_hmc},
             "map_best_chi2_per_dof": map_chi2_dof,
             "svi_loss_first_last": [float(losses[0]), float(losses[-1])],
             "hmc_accept_ratio_kept": float(acc[500:].mean()), "hmc_step_size": float(stats["step_size"][-1]),
-            "hmc_step_size_reduce": args.seq_step_reduce,
+            "hmc_step_size_reduce": args.seq_step_reduce, "svi_peak_lr": args.seq_svi_lr,
+            "hmc_leapfrog_steps_kept_mean": float(Ls[burnin:].float().mean()),
+            "hmc_graphs": stats["graphs"],
             "rhat_max": float(rhat.max()), "rhat_median": float(rhat.median()),
             "ess_min": float(ess.min()), "ess_median": float(ess.median()),
             "posterior_mean_chi2_per_dof": float(c21[0]),
             "truth_inside_95pct": "%d/%d" % (inside, tv.numel()),
             "lik_grad_evals": args.seq_map_chains * 350 + 1024 * args.seq_svi_steps
-            + args.seq_hmc_chains * 8 * (500 + args.seq_hmc_results)}
+            + args.seq_hmc_chains * int(Ls.sum())}
     print(json.dumps(line), flush=True)
 
 
@@ -682,6 +687,10 @@ def main():
     ap.add_argument("--seq-svi-steps", type=int, default=1500)
     ap.add_argument("--seq-hmc-chains", type=int, default=2048)
     ap.add_argument("--seq-hmc-results", type=int, default=1000)
+    ap.add_argument("--seq-adapt-trajectory", action="store_true",
+                    help="ChEES trajectory-length adaptation (the reference's default) instead of L = 8")
+    ap.add_argument("--seq-hmc-burnin", type=int, default=500)
+    ap.add_argument("--seq-svi-lr", type=float, default=1e-3, help="SVI peak learning rate")
     ap.add_argument("--seq-step-reduce", default="harmonic", choices=["harmonic", "mean"],
                     help="HMC step-size adaptation over chains: the reference's harmonic mean, or the mean")
     ap.add_argument("--ttm-pairs", type=int, default=2_000_000)
