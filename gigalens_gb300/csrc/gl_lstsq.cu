@@ -358,8 +358,12 @@ __global__ void __launch_bounds__(NT, 512 / NT) lsq_basis_kernel(const __grid_co
 }
 #undef GL_LSQ_CONV
 
-// pinv(G) h by cyclic Jacobi (round-robin parallel ordering), one CTA per sample.
-__global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const float* __restrict__ G,
+// pinv(G) h by cyclic Jacobi (round-robin parallel ordering), one CTA of
+// kSolveThreads per sample.  In the rotation phases thread t takes column (or
+// row) t % 64 of the pairs t / 64, t / 64 + kSolveThreads / 64, ...: no
+// runtime divisions.
+constexpr int kSolveThreads = 256;
+__global__ void __launch_bounds__(kSolveThreads) lsq_solve_kernel(int bs, int D, const float* __restrict__ G,
                                                         const float* __restrict__ h, float rcond,
                                                         float* __restrict__ coeffs, int max_sweeps,
                                                         float* __restrict__ Vout, float* __restrict__ ilam,
@@ -387,8 +391,9 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
       // convergence test: off-diagonal vs diagonal Frobenius norm (block reduction)
       {
         float off = 0.f, dg = 0.f;
-        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-          const int i = t / n, j = t - i * n;
+        for (int i = threadIdx.x >> 6; i < n; i += kSolveThreads / 64) {
+          const int j = threadIdx.x & 63;
+          if (j >= n) continue;
           const float v = A[i][j] * A[i][j];
           if (i == j) dg += v;
           else off += v;
@@ -397,15 +402,20 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
           off += __shfl_xor_sync(0xffffffffu, off, o);
           dg += __shfl_xor_sync(0xffffffffu, dg, o);
         }
-        __shared__ float wred[2][4];
+        __shared__ float wred[2][kSolveThreads / 32];
         if ((threadIdx.x & 31) == 0) {
           wred[0][threadIdx.x >> 5] = off;
           wred[1][threadIdx.x >> 5] = dg;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-          red[0] = wred[0][0] + wred[0][1] + wred[0][2] + wred[0][3];
-          red[1] = wred[1][0] + wred[1][1] + wred[1][2] + wred[1][3];
+          float o = 0.f, g = 0.f;
+          for (int w = 0; w < kSolveThreads / 32; ++w) {
+            o += wred[0][w];
+            g += wred[1][w];
+          }
+          red[0] = o;
+          red[1] = g;
         }
         __syncthreads();
       }
@@ -448,8 +458,9 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
         }
         __syncthreads();
         // rows: A <- J^T A
-        for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
-          const int k = t / n, j = t - k * n;
+        for (int k = threadIdx.x >> 6; k < npair; k += kSolveThreads / 64) {
+          const int j = threadIdx.x & 63;
+          if (j >= n) continue;
           const int p = pr[k][0], q = pr[k][1];
           const float c = cs[k][0], s = cs[k][1];
           const float ap = A[p][j], aq = A[q][j];
@@ -458,8 +469,9 @@ __global__ void __launch_bounds__(128) lsq_solve_kernel(int bs, int D, const flo
         }
         __syncthreads();
         // columns: A <- A J, V <- V J
-        for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
-          const int k = t / n, i = t - k * n;
+        for (int k = threadIdx.x >> 6; k < npair; k += kSolveThreads / 64) {
+          const int i = threadIdx.x & 63;
+          if (i >= n) continue;
           const int p = pr[k][0], q = pr[k][1];
           const float c = cs[k][0], s = cs[k][1];
           const float ap = A[i][p], aq = A[i][q];
@@ -1090,8 +1102,8 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   // least-squares problem itself
   const int xpass_blocks = std::min(bs, sms);
   const size_t xsm = xpass_smem_bytes(L->D);
-  lsq_solve_kernel<<<bs < 8 * sms ? bs : 8 * sms, 128, 0, stream>>>(bs, L->D, G, h, 1e-6f, co, 30, V, ilam,
-                                                                  status);
+  lsq_solve_kernel<<<bs < 8 * sms ? bs : 8 * sms, kSolveThreads, 0, stream>>>(bs, L->D, G, h, 1e-6f, co, 30, V,
+                                                                            ilam, status);
   for (int it = 0; it < 2; ++it) {
     lsq_xpass_kernel<false><<<xpass_blocks, kXT, xsm, stream>>>(a, co, r, nullptr, nullptr, nullptr);
     lsq_update_kernel<<<bs < 8 * sms ? bs : 8 * sms, 64, 0, stream>>>(bs, L->D, V, ilam, r, co);
