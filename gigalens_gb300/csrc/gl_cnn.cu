@@ -12,6 +12,10 @@
 
 namespace gl {
 
+// gl_cnn_tc.cu: the convolution GEMMs on the tensor cores (1: shape not handled)
+int nn_gemm_tc(int transA, int transB, int a_bf16, int M, int N, int K, float alpha, const void* A, int lda,
+               const float* B, int ldb, float* C, int ldc, int ksplit, cudaStream_t s);
+
 // ------------------------------------------------------------------ GEMM
 // C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b];  op(A) is M x K, op(B) K x N,
 // row-major storage; TA/TB select transposed storage.  A may be BF16.
@@ -302,6 +306,10 @@ int gl_nn_gemm(int transA, int transB, int a_bf16, int M, int N, int K, float al
     }
   }
   cudaStream_t s = (cudaStream_t)stream;
+  if (batch == 1 && beta == 0.f) {   // the convolution shapes run on the tensor cores
+    const int rc = nn_gemm_tc(transA, transB, a_bf16, M, N, K, alpha, A, lda, B, ldb, C, ldc, ksplit, s);
+    if (rc != 1) return rc == GL_OK ? launch_check("tensor-core gemm") : rc;
+  }
   const bool narrow = M <= 32;    // 32-channel layers: 32 x 128 tiles instead of 64 x 64
   dim3 grid(narrow ? (N + 127) / 128 : (N + 63) / 64, narrow ? (M + 31) / 32 : (M + 63) / 64, batch * ksplit);
 #define GL_GEMM(TA, TB, BF)                                                                                    \
