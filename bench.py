@@ -239,6 +239,37 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def measure_fp32_peak(torch, dev):
+    """FP32 FMA throughput (TFLOP/s) of the library's probe kernel, timed with
+    CUDA events on the current stream."""
+    from gigalens_gb300 import _native as N
+
+    stream = torch.cuda.current_stream()
+    probe_out = torch.empty(4096, device=dev)
+    flops = ctypes.c_double(0.0)
+    for _ in range(2):
+        N.call("gl_probe_fp32_fma", N.ptr(probe_out), 2000, 4, flops, N.stream_ptr())
+    pe0, pe1 = _events(torch, 2)
+    pe0.record(stream)
+    N.call("gl_probe_fp32_fma", N.ptr(probe_out), 2000, 4, flops, N.stream_ptr())
+    pe1.record(stream)
+    torch.cuda.synchronize()
+    return flops.value / (pe0.elapsed_time(pe1) * 1e-3) / 1e12
+
+
+def lstsq_flops(n, D=45, ss=2, k=21):
+    """Algorithmic FP32 flop of one least-squares evaluation of an n x n image
+    with D linear channels (the shapelet source), by component:
+    basis: 110 flop per supersampled pixel (coordinates, Hermite recursions,
+    the D products); psf: the PSF + binning of every channel, D strided
+    correlations with the (k+ss-1)^2 combined kernel at the n^2 outputs;
+    gram: A^T W A, 2 n^2 D(D+1)/2 (run as three TF32 tensor-core products,
+    counted once); rhs: A^T W b, 2 n^2 D."""
+    P, Ps, kc = n * n, (ss * n) ** 2, k + ss - 1
+    return {"basis": 110.0 * Ps, "psf": D * 2.0 * P * kc * kc,
+            "gram": 2.0 * P * D * (D + 1) / 2, "rhs": 2.0 * P * D}
+
+
 def _events(torch, n):
     return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
 
@@ -311,10 +342,15 @@ def run_lstsq_only(args):
         ev[2 * i + 1].record()
     torch.cuda.synchronize()
     t = sum(ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(args.steps)) / args.steps
+    flop = (args.lstsq_big * sum(lstsq_flops(100).values()) + args.lstsq_small * sum(lstsq_flops(60).values()))
+    achieved = flop / (t * 1e-3) / 1e12
+    peak = measure_fp32_peak(torch, dev)
     print(json.dumps({"metric": "lstsq evals/s (%d x 100^2 + %d x 60^2 px, ss=2, shapelets n_max=8, D=45)"
                                 % (args.lstsq_big, args.lstsq_small),
                       "value": nb / (t * 1e-3), "unit": "evals/s", "ms_per_step": t, "steps": args.steps,
-                      "warmup": args.warmup, "workspace_gb": wb.value / 1e9, "tuning": lsq.tuning}), flush=True)
+                      "warmup": args.warmup, "workspace_gb": wb.value / 1e9, "tuning": lsq.tuning,
+                      "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                                   "frac": achieved / peak, "flop_per_call": flop}}), flush=True)
 
 
 def run_sequence(args):
@@ -414,7 +450,7 @@ def run_sequence(args):
     print(json.dumps(line), flush=True)
 
 
-def secondary_timings(torch, dev, pm, plan, z):
+def secondary_timings(torch, dev, pm, plan, z, fp32_peak=None):
     """Quick timings of MAP, least squares and HMC at their configurations."""
     from gigalens_gb300 import _native as N
     from gigalens_gb300 import distributions as tfd
@@ -471,6 +507,19 @@ def secondary_timings(torch, dev, pm, plan, z):
     out["lstsq_evals_per_s"] = nb / (t * 1e-3)
     out["lstsq_workspace_gb"] = wb.value / 1e9
     out["lstsq_tuning"] = lsq.tuning
+    comp = {}
+    for n, cnt in ((100, 2048), (60, 512)):
+        for key, f in lstsq_flops(n).items():
+            comp[key] = comp.get(key, 0.0) + cnt * f
+    total = sum(comp.values())
+    achieved = total / (t * 1e-3) / 1e12
+    out["roofline_lstsq"] = {
+        "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+        "frac": achieved / fp32_peak if fp32_peak else None,
+        "timed": "whole gl_lstsq call (CUDA events): basis + PSF, Gram, solve, two refinement passes, image",
+        "dominant_kernel": "lsq_basis_kernel (ray trace, basis channels, PSF + binning correlation)",
+        "flop_per_call": total, "flop_components": comp,
+        "peak_source": "FP32 FMA probe kernel measured in this run"}
     del work
 
     # one fixed-length HMC iteration: 2048 chains x 8 leapfrog launches
@@ -568,16 +617,7 @@ def run_ours(args):
     value = ws * bs / (t_step * 1e-3)
 
     # ---- FP32 peak (probe kernel, same clocks)
-    probe_out = torch.empty(4096, device=dev)
-    flops = ctypes.c_double(0.0)
-    for _ in range(2):
-        N.call("gl_probe_fp32_fma", N.ptr(probe_out), 2000, 4, flops, N.stream_ptr())
-    pe0, pe1 = _events(torch, 2)
-    pe0.record(stream)
-    N.call("gl_probe_fp32_fma", N.ptr(probe_out), 2000, 4, flops, N.stream_ptr())
-    pe1.record(stream)
-    torch.cuda.synchronize()
-    fp32_peak = flops.value / (pe0.elapsed_time(pe1) * 1e-3) / 1e12
+    fp32_peak = measure_fp32_peak(torch, dev)
 
     # ---- e2e through the public API with pinned host buffers
     z_host = z.cpu().pin_memory()
@@ -611,7 +651,7 @@ def run_ours(args):
     secondary = None
     if rank == 0 and not args.no_secondary:
         del flush
-        secondary = secondary_timings(torch, dev, pm, plan, z)
+        secondary = secondary_timings(torch, dev, pm, plan, z, fp32_peak)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -458,6 +458,7 @@ int gl_device_info(int* sm_count, int* smem_optin_bytes) {
 
 int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int n_images,
                    gl_plan** out) {
+  GL_NVTX_RANGE("gl_plan_create");
   if (!model || !images || !out || n_images < 1 || n_images > GL_MAX_IMAGES) {
     set_error("gl_plan_create: bad arguments (n_images %d)", n_images);
     return GL_ERR_INVALID;
@@ -663,6 +664,7 @@ int gl_lstsq_workspace(const gl_plan* plan, int bs, size_t* bytes, int* n_channe
 int gl_lstsq(const gl_plan* plan, const float* x, const int* img_id, int bs, void* work,
              size_t work_bytes, float* coeffs, float* img_out, float* logL, float* chi2,
              void* stream) {
+  GL_NVTX_RANGE("gl_lstsq");
   if (!plan || (bs > 0 && (!x || !work || !coeffs)) || bs < 0) {
     set_error("gl_lstsq: null plan, input, workspace or coeffs");
     return GL_ERR_INVALID;
@@ -717,6 +719,7 @@ static int common_checks(const gl_plan* plan, const float* x, int bs) {
 
 int gl_forward(const gl_plan* plan, const float* x, const int* img_id, int bs, float* logL,
                float* chi2, float* img_out, int* status, void* stream) {
+  GL_NVTX_RANGE("gl_forward");
   int rc = common_checks(plan, x, bs);
   if (rc) return rc;
   if ((logL || chi2))
@@ -739,6 +742,7 @@ int gl_forward(const gl_plan* plan, const float* x, const int* img_id, int bs, f
 
 int gl_forward_grad(const gl_plan* plan, const float* x, const int* img_id, int bs, float* logL,
                     float* chi2, float* dlogL_dx, int* status, void* stream) {
+  GL_NVTX_RANGE("gl_forward_grad");
   int rc = common_checks(plan, x, bs);
   if (!rc && dlogL_dx) rc = grad_checks(plan);
   if (rc) return rc;
@@ -762,6 +766,7 @@ int gl_forward_grad(const gl_plan* plan, const float* x, const int* img_id, int 
 
 int gl_adjoint(const gl_plan* plan, const float* x, const int* img_id, int bs, const float* dlogL,
                float* dx, int* status, void* stream) {
+  GL_NVTX_RANGE("gl_adjoint");
   int rc = common_checks(plan, x, bs);
   if (!rc) rc = grad_checks(plan);
   if (rc) return rc;
@@ -783,6 +788,7 @@ int gl_adjoint(const gl_plan* plan, const float* x, const int* img_id, int bs, c
 
 int gl_log_prob(const gl_plan* plan, const float* z, const int* img_id, int bs, float* logp,
                 float* chi2, float* dlogp_dz, int* status, void* stream) {
+  GL_NVTX_RANGE("gl_log_prob");
   int rc = common_checks(plan, z, bs);
   if (!rc && dlogp_dz) rc = grad_checks(plan);
   if (rc) return rc;
@@ -826,6 +832,7 @@ int gl_autotune(const gl_plan* plan, int bs, gl_tune_result* out) {
 
 int gl_lstsq_grad(const gl_plan* plan, const float* x, const int* img_id, int bs,
                   const float* coeffs, float* logL, float* chi2, float* grad, void* stream) {
+  GL_NVTX_RANGE("gl_lstsq_grad");
   if (!plan || bs < 0 || (bs > 0 && (!x || !coeffs || !grad))) {
     set_error("gl_lstsq_grad: null plan, input, coefficients or gradient, or negative batch");
     return GL_ERR_INVALID;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "gigalens_cuda.h"
 
@@ -184,4 +185,25 @@ int launch_epl_term_count(const float* e1, const float* e2, int64_t n, int cap, 
 int launch_bijector_forward(const DevPriorLeaf* leaves, int d, const float* z, int bs, float* x,
                             cudaStream_t stream);
 void set_error(const char* fmt, ...);
+
+// Host-side NVTX range around one C-ABI call (its checks and launches), in
+// the "gigalens_gb300" domain.  NVTX v3 is header-only: without a profiler
+// attached each push/pop is a null-pointer test.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) {
+    static nvtxDomainHandle_t dom = nvtxDomainCreateA("gigalens_gb300");
+    nvtxEventAttributes_t ev = {};
+    ev.version = NVTX_VERSION;
+    ev.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+    ev.messageType = NVTX_MESSAGE_TYPE_ASCII;
+    ev.message.ascii = name;
+    domain = dom;
+    nvtxDomainRangePushEx(domain, &ev);
+  }
+  ~NvtxRange() { nvtxDomainRangePop(domain); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+  nvtxDomainHandle_t domain;
+};
+#define GL_NVTX_RANGE(name) ::gl::NvtxRange gl_nvtx_range_(name)
 }  // namespace gl

@@ -26,6 +26,7 @@ trajectory-length adaptation (Hoffman, Radul & Sountsov 2021) over the first
 one full HMC iteration (L leapfrog steps) is one CUDA graph.  TFP's random
 streams are not reproduced; the samplers are checked statistically.
 """
+import functools
 import math
 
 import numpy as np
@@ -42,9 +43,22 @@ def _cuda_dev():
     return torch.device("cuda", torch.cuda.current_device())
 
 
+def _nvtx_stage(name):
+    """An NVTX range (host side) around one driver stage, so a timeline
+    profile shows MAP, SVI and HMC beside the library's own call ranges."""
+    def wrap(fn):
+        @functools.wraps(fn)
+        def run(*args, **kwargs):
+            with torch.cuda.nvtx.range(name):
+                return fn(*args, **kwargs)
+        return run
+    return wrap
+
+
 class ModellingSequence(_inf.ModellingSequenceInterface):
     map_chi2_history = None
 
+    @_nvtx_stage("ModellingSequence.MAP")
     def MAP(self, optimizer: Adam = None, start=None, n_samples=500, num_steps=350, seed=0, use_graph=True,
             stop_chi2=None, check_every=25, distributed=False):
         """Multi-start Adam; returns the unconstrained parameters of all chains.
@@ -110,8 +124,9 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
                 torch.cuda.current_stream().wait_stream(s)
                 while done < num_steps:
                     n = min(check_every if stop_chi2 is not None else num_steps, num_steps - done)
-                    for _ in range(n):
-                        g.replay()
+                    with torch.cuda.nvtx.range("MAP steps"):
+                        for _ in range(n):
+                            g.replay()
                     done += n
                     if reached(done):
                         break
@@ -129,6 +144,7 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
         return D.global_best(self.map_z, self.map_log_prob)
 
     # ------------------------------------------------------------------ SVI
+    @_nvtx_stage("ModellingSequence.SVI")
     def SVI(self, optimizer, start, n_vi=250, init_scales=1e-3, num_steps=500, seed=2, use_graph=True,
             distributed=False):
         """Returns ``(q_z, losses)`` like the reference (unconstrained space).
@@ -193,6 +209,7 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
         return q_z, losses[:num_steps]
 
     # ------------------------------------------------------------------ HMC
+    @_nvtx_stage("ModellingSequence.HMC")
     def HMC(self, q_z, init_eps=0.3, init_l=3, n_hmc=50, num_burnin_steps=250, num_results=750,
             max_leapfrog_steps=30, seed=3, adapt_trajectory=True, adapt_step_size=True,
             target_accept_prob=0.75, use_graph=True, distributed=False, step_size_reduce="harmonic"):
@@ -314,6 +331,7 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
 
         for it in range(total):
             adapting = it < n_adapt
+            torch.cuda.nvtx.range_push("HMC iteration")
             run(("pre", adapting), pre(adapting))
             if chees is not None:
                 L_host.copy_(chees.L_dev, non_blocking=False)
@@ -325,6 +343,7 @@ class ModellingSequence(_inf.ModellingSequenceInterface):
             run(("post", adapting, it == n_adapt), post(adapting, it == n_adapt))
             if it >= num_burnin_steps:
                 samples[it - num_burnin_steps].copy_(z)
+            torch.cuda.nvtx.range_pop()
         stats = {"accept_ratio": acc_trace, "step_size": eps_trace,
                  "leapfrog_steps": torch.tensor(L_trace), "target_log_prob": logp,
                  "graphs": len(graphs)}

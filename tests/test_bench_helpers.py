@@ -30,3 +30,16 @@ def test_flop_count_of_the_headline_workload():
     Ps, P = 180 * 180, 90 * 90
     assert fwd == Ps * (84 + 310) + 2 * P * 42 ** 2 + 12 * P
     assert adj - fwd == Ps * (84 + 310)
+
+
+def test_flop_count_of_the_least_squares_workload():
+    """100x100 px, ss = 2, 21x21 supersampled PSF (22x22 combined kernel),
+    45 shapelet channels: basis 110 per supersampled pixel, 45 strided
+    correlations, A^T W A counted once, A^T W b."""
+    f = bench.lstsq_flops(100)
+    P = 100 * 100
+    assert f["basis"] == 110 * 200 * 200
+    assert f["psf"] == 45 * 2 * P * 22 ** 2
+    assert f["gram"] == 2 * P * 45 * 46 / 2
+    assert f["rhs"] == 2 * P * 45
+    assert sum(f.values()) == 461_600_000
