@@ -353,6 +353,118 @@ def run_lstsq_only(args):
                                    "frac": achieved / peak, "flop_per_call": flop}}), flush=True)
 
 
+def run_general_path(args):
+    """Rate of the general-path kernels beside the headline family: one
+    gl_forward_grad (likelihood + gradient, physical parameters) per step for
+    4096 chains of the 90^2 px configuration, per model:
+      headline            EPL + shear ; SersicEllipse ; SersicEllipse  (family 0)
+      sie_shear_se_se     SIE + shear ; SersicEllipse ; SersicEllipse  (compiled signature 5)
+      sis_shear_se_se     SIS + shear ; SersicEllipse ; SersicEllipse  (compiled signature 6)
+      sie_sis_shear_se_se SIE + SIS(theta_E = 1e-4) + shear ; ... (run-time general path 4)
+      epl_sis_shear_se_se the headline model + SIS(theta_E = 1e-4) (run-time general path 4)
+    and the BackwardProbModel gradient (gl_lstsq_grad) of EPL + shear with a
+    shapelet source (n_max 8) at 100^2 px, 2048 chains, compiled signature 7,
+    against the same model with a Sersic lens light (run-time path 4)."""
+    import torch
+
+    from gigalens_gb300 import _native as N
+    from gigalens_gb300 import workloads as W
+    from gigalens_gb300.model import PhysicalModel
+    from gigalens_gb300.simulator import SimulatorConfig
+    from gigalens_gb300.cuda._plan import ModelLayout, Plan
+    from gigalens_gb300.cuda.profiles.light import sersic, shapelets
+    from gigalens_gb300.cuda.profiles.mass import epl, shear, sie, sis
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    bs = args.chains
+    cfg = W.config1()
+    xs = W.draw_params(bs, seed=1)
+    lens, sh, ll, src = xs[0][0], xs[0][1], xs[1][0], xs[2][0]
+    sie_p = {k: lens[k] for k in ("theta_E", "e1", "e2", "center_x", "center_y")}
+    sis_p = {k: lens[k] for k in ("theta_E", "center_x", "center_y")}
+    tiny = {"theta_E": torch.full((bs,), 1e-4), "center_x": torch.zeros(bs), "center_y": torch.zeros(bs)}
+    models = {
+        "headline": ([epl.EPL(W.NITER), shear.Shear()], [[lens, sh], [ll], [src]]),
+        "sie_shear_se_se": ([sie.SIE(), shear.Shear()], [[sie_p, sh], [ll], [src]]),
+        "sis_shear_se_se": ([sis.SIS(), shear.Shear()], [[sis_p, sh], [ll], [src]]),
+        "sie_sis_shear_se_se": ([sie.SIE(), sis.SIS(), shear.Shear()], [[sie_p, tiny, sh], [ll], [src]]),
+        "epl_sis_shear_se_se": ([epl.EPL(W.NITER), sis.SIS(), shear.Shear()], [[lens, tiny, sh], [ll], [src]]),
+    }
+    obs = np.random.default_rng(0).normal(scale=0.2, size=(N_PIX, N_PIX)).astype(np.float32) + 1.0
+    out = {}
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = _events(torch, 2)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for name, (mass, params) in models.items():
+        phys = PhysicalModel(mass, [sersic.SersicEllipse()], [sersic.SersicEllipse()])
+        lay = ModelLayout(phys)
+        plan = Plan(lay, [dict(sim_config=cfg, observed=obs, background_rms=W.BG_RMS, exp_time=W.EXP_TIME)])
+        x = lay.flatten_params(params).to(dev).contiguous()
+        logL, chi2, grad = torch.empty(bs, device=dev), torch.empty(bs, device=dev), torch.empty_like(x)
+
+        def step():
+            N.call("gl_forward_grad", plan.handle, N.ptr(x), None, bs, N.ptr(logL), N.ptr(chi2), N.ptr(grad),
+                   None, N.stream_ptr())
+
+        ms = timed(step, args.steps)
+        lc = plan.launch_config(bs)
+        out[name] = {"ms": ms, "evals_per_s": bs / (ms * 1e-3), "family": lc["family"],
+                     "global_planes": lc["global_planes"], "finite": bool(torch.isfinite(grad).all())}
+    ref = out["headline"]["evals_per_s"]
+    for v in out.values():
+        v["of_headline"] = v["evals_per_s"] / ref
+
+    # BackwardProbModel gradient: shapelet source n_max = 8 at 100^2 px
+    nb = 2048
+    r = np.random.default_rng(3)
+    shp = {"beta": torch.tensor(r.uniform(0.05, 0.2, nb), dtype=torch.float32),
+           "center_x": torch.tensor(r.normal(0, 0.05, nb), dtype=torch.float32),
+           "center_y": torch.tensor(r.normal(0, 0.05, nb), dtype=torch.float32)}
+    lp = W.draw_params(nb, seed=4)
+    cfg100 = SimulatorConfig(delta_pix=W.DELTA_PIX, num_pix=100, supersample=2,
+                             kernel_supersampled=W.gaussian_psf(W.FWHM, W.DELTA_PIX / 2, 21))
+    o100 = np.random.default_rng(100).normal(scale=0.1, size=(100, 100)).astype(np.float32) + 0.5
+    ll_l = {k: v for k, v in lp[1][0].items() if k != "Ie"}
+    for name, light, params in (
+            ("lstsq_grad_epl_shear_shp", [], [[lp[0][0], lp[0][1]], [shp]]),
+            ("lstsq_grad_epl_shear_se_shp", [sersic.SersicEllipse(use_lstsq=True)],
+             [[lp[0][0], lp[0][1]], [ll_l], [shp]])):
+        phys = PhysicalModel([epl.EPL(W.NITER), shear.Shear()], light,
+                             [shapelets.Shapelets(8, use_lstsq=True, interpolate=False)])
+        lay = ModelLayout(phys)
+        plan = Plan(lay, [dict(sim_config=cfg100, observed=o100, background_rms=0.1, exp_time=200.0)])
+        x = lay.flatten_params(params).to(dev).contiguous()
+        wb, D = ctypes.c_size_t(0), ctypes.c_int(0)
+        N.call("gl_lstsq_workspace", plan.handle, nb, ctypes.byref(wb), ctypes.byref(D))
+        work = torch.empty(wb.value, dtype=torch.uint8, device=dev)
+        co = torch.empty(nb, D.value, device=dev)
+        lg = torch.empty(nb, device=dev)
+        N.call("gl_lstsq", plan.handle, N.ptr(x), None, nb, N.ptr(work), wb.value, N.ptr(co), None, N.ptr(lg),
+               None, N.stream_ptr())
+        del work
+        grad = torch.empty_like(x)
+
+        def gstep():
+            N.call("gl_lstsq_grad", plan.handle, N.ptr(x), None, nb, N.ptr(co), N.ptr(lg), None, N.ptr(grad),
+                   N.stream_ptr())
+
+        ms = timed(gstep, max(3, args.steps // 4))
+        out[name] = {"ms": ms, "evals_per_s": nb / (ms * 1e-3), "finite": bool(torch.isfinite(grad).all())}
+    print(json.dumps({"metric": "general-path lik+grad evals/s (%d x 90^2 px; lstsq grad 2048 x 100^2 px)" % bs,
+                      "unit": "evals/s", "steps": args.steps, "warmup": args.warmup, "models": out}), flush=True)
+
+
 def run_sequence(args):
     """The full modelling sequence at 90x90 px (ss = 2, 41x41 supersampled
     PSF): MAP (4096 prior-draw chains, Adam lr 5e-3, 350 steps) -> SVI from
@@ -721,6 +833,9 @@ def main():
     ap.add_argument("--lstsq-small", type=int, default=512, help="samples of the 60x60 image")
     ap.add_argument("--lstsq-ctas", type=int, default=0, help="basis kernel CTAs per SM (1 or 2; 0: plan default)")
     ap.add_argument("--lstsq-cb", type=int, default=0, help="basis correlation column block (16, 20; 0: planner)")
+    ap.add_argument("--general-path", action="store_true",
+                    help="time the general-path kernels (compiled signatures and run-time dispatch) beside the "
+                         "headline family")
     ap.add_argument("--sequence", action="store_true",
                     help="run the full MAP -> SVI -> HMC sequence at 90^2 px (about two minutes)")
     ap.add_argument("--seq-map-chains", type=int, default=4096)
@@ -743,6 +858,8 @@ def main():
         run_reference(args)
     elif args.lstsq_only:
         run_lstsq_only(args)
+    elif args.general_path:
+        run_general_path(args)
     elif args.sequence:
         run_sequence(args)
     else:

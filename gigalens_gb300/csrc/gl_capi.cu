@@ -223,6 +223,22 @@ static int resolve_generic(const gl_model_desc* m, bool lsq, GenArgs* g, DevProf
   return GL_OK;
 }
 
+// The compiled general-path signature matching the model of g (the profile
+// types, counts, light groups and the shear), or FAM_GENERIC.
+static int gen_signature(const GenArgs& g) {
+  if (!g.has_shear || g.n_mass != 1) return FAM_GENERIC;
+  const int m = g.mass[0].type;
+  if (g.n_light == 2 && g.light[0].type == GL_PROF_SERSIC_ELLIPSE && g.light[0].group == GL_GROUP_LENS_LIGHT &&
+      g.light[1].type == GL_PROF_SERSIC_ELLIPSE && g.light[1].group == GL_GROUP_SOURCE) {
+    if (m == GL_PROF_SIE) return FAM_SIG_SIE_SHEAR_SE_SE;
+    if (m == GL_PROF_SIS) return FAM_SIG_SIS_SHEAR_SE_SE;
+  }
+  if (g.n_light == 1 && m == GL_PROF_EPL && g.light[0].type == GL_PROF_SHAPELETS &&
+      g.light[0].group == GL_GROUP_SOURCE)
+    return FAM_SIG_EPL_SHEAR_SHP;
+  return FAM_GENERIC;
+}
+
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 struct HostImage {
@@ -497,16 +513,19 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
     // the general path with the coefficients as amplitudes (gl_lstsq_grad)
     DevProfile e, sh;
     plan->gen_ok = resolve_generic(model, true, &plan->gen, &e, &sh) == GL_OK;
+    plan->gen_family = FAM_GENERIC;
     if (plan->gen_ok) {
       plan->epl = e;
       plan->shear = sh;
+      plan->gen_family = gen_signature(plan->gen);
     }
     set_error("");
   } else if (!resolve_family(model, &plan->family, &plan->epl, &plan->shear, &plan->llight,
                              &plan->source)) {
     rc = resolve_generic(model, false, &plan->gen, &plan->epl, &plan->shear);
-    plan->family = FAM_GENERIC;
     plan->gen_ok = rc == GL_OK;
+    plan->family = plan->gen_ok ? gen_signature(plan->gen) : FAM_GENERIC;
+    plan->gen_family = plan->family;
   }
   if (!rc && plan->epl.type == GL_PROF_EPL && (plan->epl.niter < 0 || plan->epl.niter > kMaxTerms)) {
     set_error("EPL niter %d outside [0, %d]", plan->epl.niter, kMaxTerms);
@@ -547,13 +566,15 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
   // per-thread accumulator arrays live in local memory, which hits L1 only
   // when shared memory is not carved out for the planes (90^2 px: 262 k ->
   // 288 k evals/s).
-  if (plan->family == FAM_GENERIC || (lsq_model && plan->gen_ok)) plan->fused_fits = 0;
+  // The compiled signatures keep them in shared memory when they fit.
+  if (plan->family == FAM_GENERIC || (lsq_model && plan->gen_ok && plan->gen_family == FAM_GENERIC))
+    plan->fused_fits = 0;
   rc = cuda_check(cudaMalloc((void**)&plan->dev_buf, bytes), "cudaMalloc(plan)");
   if (rc) {
     delete plan;
     return rc;
   }
-  if (!plan->fused_fits && !lsq_model && plan->family != FAM_GENERIC &&
+  if (!plan->fused_fits && !lsq_model && !is_gen_family(plan->family) &&
       plan->family != FAM_EPL_SHEAR_SE_SE) {
     // planes in global memory: the headline family and the general path
     rc = resolve_generic(model, false, &plan->gen, &plan->epl, &plan->shear);
@@ -562,7 +583,8 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
       delete plan;
       return rc;
     }
-    plan->family = FAM_GENERIC;
+    plan->family = gen_signature(plan->gen);
+    plan->gen_family = plan->family;
     plan->gen_ok = 1;
   }
   if (!plan->fused_fits && (!lsq_model || plan->gen_ok)) {
@@ -601,7 +623,7 @@ int gl_plan_create(const gl_model_desc* model, const gl_image_desc* images, int 
     if (model->prof[i].type == GL_PROF_SHAPELETS && model->prof[i].interpolate && !plan->shp_tab)
       rc = shapelet_table(plan->device, &plan->shp_tab);
   plan->gen.shp_tab = plan->shp_tab;
-  if (!rc && plan->fused_fits) rc = fused_kernel_prepare(plan->smem_bytes);
+  if (!rc && plan->fused_fits && (!lsq_model || plan->gen_ok)) rc = fused_kernel_prepare(plan->smem_bytes);
   if (!rc && lsq_model) {
     std::vector<std::vector<float>> errs(n_images);
     for (int i = 0; i < n_images; ++i) errs[i] = hi[i].err;
@@ -697,7 +719,7 @@ int gl_plan_query(const gl_plan* plan, int* smem_bytes, int* threads_per_block, 
 }
 
 static int grad_checks(const gl_plan* plan) {
-  if (plan->family == FAM_GENERIC && plan->gen.explicit_shapelets > 1) {
+  if (is_gen_family(plan->family) && plan->gen.explicit_shapelets > 1) {
     set_error("gradients with respect to the amplitudes of more than one explicit shapelet "
               "profile are not implemented; use Shapelets(use_lstsq=True)");
     return GL_ERR_UNSUPPORTED;
@@ -854,7 +876,7 @@ int gl_lstsq_grad(const gl_plan* plan, const float* x, const int* img_id, int bs
     }
   FusedArgs a;
   fill_args(plan, a);
-  a.family = FAM_GENERIC;
+  a.family = plan->gen_family;
   a.gen.amps = coeffs;
   a.gen.noise_err = 1;
   a.gen.unit_cf = 1;

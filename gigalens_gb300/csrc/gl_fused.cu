@@ -15,7 +15,8 @@ static int g_smem_set[kMaxDevices];   // dynamic smem attribute set per device (
 int fused_static_smem_bytes() {
   return std::max({fam_static_smem<FAM_EPL_SHEAR_SE_SE>(), fam_static_smem<FAM_EPL_SHEAR_SE>(),
                    fam_static_smem<FAM_EPL_SE_SE>(), fam_static_smem<FAM_EPL_SE>(),
-                   fam_static_smem<FAM_GENERIC>()});
+                   fam_static_smem<FAM_GENERIC>(), fam_static_smem<FAM_SIG_SIE_SHEAR_SE_SE>(),
+                   fam_static_smem<FAM_SIG_SIS_SHEAR_SE_SE>(), fam_static_smem<FAM_SIG_EPL_SHEAR_SHP>()});
 }
 
 int fused_kernel_prepare(int smem_bytes) {
@@ -26,6 +27,9 @@ int fused_kernel_prepare(int smem_bytes) {
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SE_SE>(smem_bytes);
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SE>(smem_bytes);
   if (e == cudaSuccess) e = fam_set_smem<FAM_EPL_SHEAR_SE_SE, false>(smem_bytes);
+  if (e == cudaSuccess) e = fam_set_smem<FAM_SIG_SIE_SHEAR_SE_SE>(smem_bytes);
+  if (e == cudaSuccess) e = fam_set_smem<FAM_SIG_SIS_SHEAR_SE_SE>(smem_bytes);
+  if (e == cudaSuccess) e = fam_set_smem<FAM_SIG_EPL_SHEAR_SHP>(smem_bytes);
   if (e != cudaSuccess) {
     set_error("cudaFuncSetAttribute(max dynamic smem %d): %s", smem_bytes, cudaGetErrorString(e));
     return GL_ERR_CUDA;
@@ -51,6 +55,9 @@ int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream) {
     switch (a.family) {
       case FAM_EPL_SHEAR_SE_SE: fam_launch<FAM_EPL_SHEAR_SE_SE, true>(a, grid, 0, stream); break;
       case FAM_GENERIC: fam_launch<FAM_GENERIC, true>(a, grid, 0, stream); break;
+      case FAM_SIG_SIE_SHEAR_SE_SE: fam_launch<FAM_SIG_SIE_SHEAR_SE_SE, true>(a, grid, 0, stream); break;
+      case FAM_SIG_SIS_SHEAR_SE_SE: fam_launch<FAM_SIG_SIS_SHEAR_SE_SE, true>(a, grid, 0, stream); break;
+      case FAM_SIG_EPL_SHEAR_SHP: fam_launch<FAM_SIG_EPL_SHEAR_SHP, true>(a, grid, 0, stream); break;
       default:
         set_error("model family %d has no global-memory plane kernel", a.family);
         return GL_ERR_INVALID;
@@ -66,6 +73,13 @@ int launch_fused(const FusedArgs& a, int smem_bytes, cudaStream_t stream) {
       case FAM_EPL_SHEAR_SE: fam_launch<FAM_EPL_SHEAR_SE, false>(a, grid, smem_bytes, stream); break;
       case FAM_EPL_SE_SE: fam_launch<FAM_EPL_SE_SE, false>(a, grid, smem_bytes, stream); break;
       case FAM_EPL_SE: fam_launch<FAM_EPL_SE, false>(a, grid, smem_bytes, stream); break;
+      case FAM_SIG_SIE_SHEAR_SE_SE:
+        fam_launch<FAM_SIG_SIE_SHEAR_SE_SE, false>(a, grid, smem_bytes, stream);
+        break;
+      case FAM_SIG_SIS_SHEAR_SE_SE:
+        fam_launch<FAM_SIG_SIS_SHEAR_SE_SE, false>(a, grid, smem_bytes, stream);
+        break;
+      case FAM_SIG_EPL_SHEAR_SHP: fam_launch<FAM_SIG_EPL_SHEAR_SHP, false>(a, grid, smem_bytes, stream); break;
       case FAM_GENERIC:
         set_error("the general path needs the plan's global plane scratch");
         return GL_ERR_INVALID;

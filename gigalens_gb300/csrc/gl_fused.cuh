@@ -52,6 +52,75 @@ struct FamTraits<FAM_GENERIC> {
   static constexpr bool kShear = false, kLensLight = false;   // unused: runtime lists
 };
 
+// Model signature of the general-path kernels: the mass and light profile
+// types, the light groups and the shear.  FAM_GENERIC reads them from GenArgs
+// at run time and keeps the per-profile reverse code out of line; the
+// compiled signatures (FAM_SIG_*) fix them at compile time, so the profile
+// code is inlined per slot and the gradient accumulators stay in registers.
+// Column maps, amplitudes and every other per-profile setting still come from
+// GenArgs.
+template <int FAM>
+struct GenSig {
+  static constexpr bool kStatic = false;
+  static constexpr bool kShear = false;
+  static constexpr int kNMass = 0, kNLight = 0;
+  __device__ static constexpr int mass(int) { return GL_PROF_NONE; }
+  __device__ static constexpr int light(int) { return GL_PROF_NONE; }
+  __device__ static constexpr bool src(int) { return false; }
+};
+template <>
+struct GenSig<FAM_SIG_SIE_SHEAR_SE_SE> {   // SIE + shear ; SersicEllipse ; SersicEllipse
+  static constexpr bool kStatic = true, kShear = true;
+  static constexpr int kNMass = 1, kNLight = 2;
+  __device__ static constexpr int mass(int s) { return s == 0 ? GL_PROF_SIE : GL_PROF_NONE; }
+  __device__ static constexpr int light(int l) { return l < 2 ? GL_PROF_SERSIC_ELLIPSE : GL_PROF_NONE; }
+  __device__ static constexpr bool src(int l) { return l == 1; }
+};
+template <>
+struct GenSig<FAM_SIG_SIS_SHEAR_SE_SE> {   // SIS + shear ; SersicEllipse ; SersicEllipse
+  static constexpr bool kStatic = true, kShear = true;
+  static constexpr int kNMass = 1, kNLight = 2;
+  __device__ static constexpr int mass(int s) { return s == 0 ? GL_PROF_SIS : GL_PROF_NONE; }
+  __device__ static constexpr int light(int l) { return l < 2 ? GL_PROF_SERSIC_ELLIPSE : GL_PROF_NONE; }
+  __device__ static constexpr bool src(int l) { return l == 1; }
+};
+template <>
+struct GenSig<FAM_SIG_EPL_SHEAR_SHP> {     // EPL + shear ; no lens light ; Shapelets
+  static constexpr bool kStatic = true, kShear = true;
+  static constexpr int kNMass = 1, kNLight = 1;
+  __device__ static constexpr int mass(int s) { return s == 0 ? GL_PROF_EPL : GL_PROF_NONE; }
+  __device__ static constexpr int light(int l) { return l == 0 ? GL_PROF_SHAPELETS : GL_PROF_NONE; }
+  __device__ static constexpr bool src(int l) { return l == 0; }
+};
+template <int FAM>
+constexpr bool kGenFamily = FAM >= FAM_GENERIC;
+
+// Signature accessors: compile-time for the compiled signatures.
+template <class S>
+__device__ __forceinline__ int gs_n_mass(const GenArgs& g) {
+  if constexpr (S::kStatic) return S::kNMass; else return g.n_mass;
+}
+template <class S>
+__device__ __forceinline__ int gs_mass(const GenArgs& g, int s) {
+  if constexpr (S::kStatic) return S::mass(s); else return g.mass[s].type;
+}
+template <class S>
+__device__ __forceinline__ bool gs_shear(const GenArgs& g) {
+  if constexpr (S::kStatic) return S::kShear; else return g.has_shear != 0;
+}
+template <class S>
+__device__ __forceinline__ int gs_n_light(const GenArgs& g) {
+  if constexpr (S::kStatic) return S::kNLight; else return g.n_light;
+}
+template <class S>
+__device__ __forceinline__ int gs_light(const GenArgs& g, int l) {
+  if constexpr (S::kStatic) return S::light(l); else return g.light[l].type;
+}
+template <class S>
+__device__ __forceinline__ bool gs_src(const GenArgs& g, int l) {
+  if constexpr (S::kStatic) return S::src(l); else return g.light[l].group == GL_GROUP_SOURCE;
+}
+
 // Pixels per thread whose series recurrences interleave (phase 1, phase 4).
 constexpr int kPixF = 4;
 constexpr int kPixR = 2;
@@ -66,6 +135,7 @@ struct SmemStatic {
   int K[GL_MAX_IMAGES];
   // general path
   SerC gser[kGenLight];            // Sersic constants of the light slots
+  SieC gsie[kGenMass];             // SIE constants of the mass slots
   float amp[kMaxAmps];             // external amplitudes of the current sample
   float ampg[64];                  // d logL / d (explicit shapelet amplitudes)
   float pref[kMaxShapeletN + 1];   // shapelet normalisations 1/sqrt(2^n sqrt(pi) n!)
@@ -609,16 +679,16 @@ __device__ __forceinline__ float gen_amp(const GenLight& L, const SmemStatic& st
 }
 
 // Deflection of a non-EPL mass slot (value only).
-__device__ __forceinline__ void gen_mass_alpha(const DevProfile& m, const float* sx, float x,
-                                               float y, float& ax, float& ay) {
+__device__ __forceinline__ void gen_mass_alpha(const DevProfile& m, int type, int slot, const SmemStatic& st,
+                                               float x, float y, float& ax, float& ay) {
+  const float* sx = st.x;
   const int* c = m.col;
-  switch (m.type) {
+  switch (type) {
     case GL_PROF_SIS:
       sis_alpha_t<float>(pget(sx, c[0], 0.f), pget(sx, c[1], 0.f), pget(sx, c[2], 0.f), x, y, ax, ay);
       break;
     case GL_PROF_SIE:
-      sie_alpha_t<float>(pget(sx, c[0], 0.f), pget(sx, c[1], 0.f), pget(sx, c[2], 0.f),
-                         pget(sx, c[3], 0.f), pget(sx, c[4], 0.f), x, y, ax, ay);
+      sie_alpha(st.gsie[slot], x, y, ax, ay);
       break;
     case GL_PROF_TNFW:
       tnfw_alpha_t<float>(pget(sx, c[0], 1.f), pget(sx, c[1], 0.f), pget(sx, c[2], 1.f),
@@ -631,23 +701,23 @@ __device__ __forceinline__ void gen_mass_alpha(const DevProfile& m, const float*
 
 // d(alpha)/d(parameters) of a non-EPL mass slot contracted with the
 // deflection adjoint (abx, aby), added to acc[0..4].
-static __device__ __noinline__ void gen_mass_reverse(const DevProfile& m, const float* sx, float x,
-                                                 float y, float abx, float aby, float* acc) {
+__device__ __forceinline__ void gen_mass_reverse_body(const DevProfile& m, int type, int slot,
+                                                      const SmemStatic& st, float x, float y, float abx,
+                                                      float aby, float* acc) {
   using D5 = Dual<5>;
+  const float* sx = st.x;
   const int* c = m.col;
   D5 ax, ay;
   int np = 0;
-  switch (m.type) {
+  if (type == GL_PROF_SIE) {   // hand-written reverse mode: adjoints of the per-sample intermediates
+    sie_backprop(st.gsie[slot], x, y, abx, aby, acc);
+    return;
+  }
+  switch (type) {
     case GL_PROF_SIS:
       np = 3;
       sis_alpha_t<D5>(D5::seed(pget(sx, c[0], 0.f), 0), D5::seed(pget(sx, c[1], 0.f), 1),
                       D5::seed(pget(sx, c[2], 0.f), 2), x, y, ax, ay);
-      break;
-    case GL_PROF_SIE:
-      np = 5;
-      sie_alpha_t<D5>(D5::seed(pget(sx, c[0], 0.f), 0), D5::seed(pget(sx, c[1], 0.f), 1),
-                      D5::seed(pget(sx, c[2], 0.f), 2), D5::seed(pget(sx, c[3], 0.f), 3),
-                      D5::seed(pget(sx, c[4], 0.f), 4), x, y, ax, ay);
       break;
     case GL_PROF_TNFW:
       np = 5;
@@ -662,13 +732,18 @@ static __device__ __noinline__ void gen_mass_reverse(const DevProfile& m, const 
   for (int k = 0; k < 5; ++k)
     if (k < np) acc[k] += abx * ax.d[k] + aby * ay.d[k];
 }
+// Out-of-line form for the run-time signature.
+static __device__ __noinline__ void gen_mass_reverse(const DevProfile& m, int slot, const SmemStatic& st,
+                                                 float x, float y, float abx, float aby, float* acc) {
+  gen_mass_reverse_body(m, m.type, slot, st, x, y, abx, aby, acc);
+}
 
 // Value of light slot l at (X, Y).
-__device__ __forceinline__ float gen_light(const GenLight& L, int l, const SmemStatic& st, const float* tab,
-                                           float X, float Y) {
+__device__ __forceinline__ float gen_light(const GenLight& L, int type, int l, const SmemStatic& st,
+                                           const float* tab, float X, float Y) {
   const float* sx = st.x;
   const int* c = L.col;
-  switch (L.type) {
+  switch (type) {
     case GL_PROF_SERSIC_ELLIPSE:
       return sersic_light(st.gser[l], X, Y);
     case GL_PROF_CORE_SERSIC:
@@ -690,12 +765,12 @@ __device__ __forceinline__ float gen_light(const GenLight& L, int l, const SmemS
 
 // Reverse of light slot l at (X, Y) with image adjoint gi: parameter adjoints
 // into acc[0..9], evaluation-point adjoint into (Xb, Yb).
-static __device__ __noinline__ void gen_light_reverse(const GenLight& L, int l, const SmemStatic& st,
-                                                  const float* tab, float X, float Y, float gi, float* acc,
-                                                  float& Xb, float& Yb) {
+__device__ __forceinline__ void gen_light_reverse_body(const GenLight& L, int type, int l, const SmemStatic& st,
+                                                       const float* tab, float X, float Y, float gi, float* acc,
+                                                       float& Xb, float& Yb) {
   const float* sx = st.x;
   const int* c = L.col;
-  switch (L.type) {
+  switch (type) {
     case GL_PROF_SERSIC_ELLIPSE: {
       const SerFwd f = sersic_fwd(st.gser[l], X, Y);
       SerAcc a;
@@ -751,13 +826,22 @@ static __device__ __noinline__ void gen_light_reverse(const GenLight& L, int l, 
   }
 }
 
-// Phase 1 (general path).
+// Out-of-line form for the run-time signature.
+static __device__ __noinline__ void gen_light_reverse(const GenLight& L, int l, const SmemStatic& st,
+                                                  const float* tab, float X, float Y, float gi, float* acc,
+                                                  float& Xb, float& Yb) {
+  gen_light_reverse_body(L, L.type, l, st, tab, X, Y, gi, acc, Xb, Yb);
+}
+
+// Phase 1 (general path), signature S.
+template <class S>
 static __device__ void phase_pixels_forward_gen(const FusedArgs& a, const DevImage& I, float* sm,
                                          const SmemStatic& st, int K) {
   const GenArgs& g = a.gen;
   const EplC ec = gen_epl_consts(g, st.x, K);
-  const float g1 = g.has_shear ? pget(st.x, a.shear.col[0], 0.f) : 0.f;
-  const float g2 = g.has_shear ? pget(st.x, a.shear.col[1], 0.f) : 0.f;
+  const bool has_shear = gs_shear<S>(g);
+  const float g1 = has_shear ? pget(st.x, a.shear.col[0], 0.f) : 0.f;
+  const float g2 = has_shear ? pget(st.x, a.shear.col[1], 0.f) : 0.f;
   const int total = I.nplanes * I.N * I.N;
   const float4* grid = reinterpret_cast<const float4*>(I.grid);
   for (int px = threadIdx.x; px < total; px += kThreads) {
@@ -765,31 +849,32 @@ static __device__ void phase_pixels_forward_gen(const FusedArgs& a, const DevIma
     float ax = 0.f, ay = 0.f;
 #pragma unroll
     for (int s = 0; s < kGenMass; ++s) {
-      if (s < g.n_mass) {
+      if (s < gs_n_mass<S>(g)) {
         float mx, my;
-        if (g.mass[s].type == GL_PROF_EPL) {
+        const int mt = gs_mass<S>(g, s);
+        if (mt == GL_PROF_EPL) {
           float xs[1] = {xy.x}, ys[1] = {xy.y}, ox[1], oy[1];
           epl_deflect_n<1>(ec, st.tab, xs, ys, ox, oy);
           mx = ox[0];
           my = oy[0];
         } else {
-          gen_mass_alpha(g.mass[s], st.x, xy.x, xy.y, mx, my);
+          gen_mass_alpha(g.mass[s], mt, s, st, xy.x, xy.y, mx, my);
         }
         ax += mx;
         ay += my;
       }
     }
     float bx = xy.x - ax, by = xy.y - ay;
-    if (g.has_shear) {
+    if (has_shear) {
       bx = bx - (g1 * xy.x + g2 * xy.y);
       by = by - (g2 * xy.x - g1 * xy.y);
     }
     float img = 0.f;
 #pragma unroll
     for (int l = 0; l < kGenLight; ++l)
-      if (l < g.n_light) {
-        const bool src = g.light[l].group == GL_GROUP_SOURCE;
-        img += gen_light(g.light[l], l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y);
+      if (l < gs_n_light<S>(g)) {
+        const bool src = gs_src<S>(g, l);
+        img += gen_light(g.light[l], gs_light<S>(g, l), l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y);
       }
     if (isnan(img)) img = 0.f;
     sm[__float_as_int(xy.z)] = img;
@@ -854,13 +939,15 @@ static __device__ __forceinline__ void shapelet_amp_grad(float g, float u, float
   }
 }
 
-// Phase 4 (general path).
+// Phase 4 (general path), signature S.
+template <class S>
 static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevImage& I, const float* sm,
                                          SmemStatic& st, int K) {
   const GenArgs& g = a.gen;
   const EplC ec = gen_epl_consts(g, st.x, K);
-  const float g1 = g.has_shear ? pget(st.x, a.shear.col[0], 0.f) : 0.f;
-  const float g2 = g.has_shear ? pget(st.x, a.shear.col[1], 0.f) : 0.f;
+  const bool has_shear = gs_shear<S>(g);
+  const float g1 = has_shear ? pget(st.x, a.shear.col[0], 0.f) : 0.f;
+  const float g2 = has_shear ? pget(st.x, a.shear.col[1], 0.f) : 0.f;
   float acc[G_NACC];
 #pragma unroll
   for (int k = 0; k < G_NACC; ++k) acc[k] = 0.f;
@@ -883,30 +970,31 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
     float ax = 0.f, ay = 0.f;
 #pragma unroll
     for (int s = 0; s < kGenMass; ++s) {
-      if (s < g.n_mass) {
+      if (s < gs_n_mass<S>(g)) {
         float mx, my;
-        if (g.mass[s].type == GL_PROF_EPL) {
+        const int mt = gs_mass<S>(g, s);
+        if (mt == GL_PROF_EPL) {
           es = epl_state(ec, st.tab, xy.x, xy.y);
           mx = es.ax;
           my = es.ay;
         } else {
-          gen_mass_alpha(g.mass[s], st.x, xy.x, xy.y, mx, my);
+          gen_mass_alpha(g.mass[s], mt, s, st, xy.x, xy.y, mx, my);
         }
         ax += mx;
         ay += my;
       }
     }
     float bx = xy.x - ax, by = xy.y - ay;
-    if (g.has_shear) {
+    if (has_shear) {
       bx = bx - (g1 * xy.x + g2 * xy.y);
       by = by - (g2 * xy.x - g1 * xy.y);
     }
     float img = 0.f;
 #pragma unroll
     for (int l = 0; l < kGenLight; ++l)
-      if (l < g.n_light) {
-        const bool src = g.light[l].group == GL_GROUP_SOURCE;
-        img += gen_light(g.light[l], l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y);
+      if (l < gs_n_light<S>(g)) {
+        const bool src = gs_src<S>(g, l);
+        img += gen_light(g.light[l], gs_light<S>(g, l), l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y);
       }
     if (!isnan(img)) {   // the reference zeroes NaN pixels: no gradient flows
     if (as >= 0) {
@@ -921,28 +1009,34 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
     float bxb = 0.f, byb = 0.f;
 #pragma unroll
     for (int l = 0; l < kGenLight; ++l)
-      if (l < g.n_light) {
-        const bool src = g.light[l].group == GL_GROUP_SOURCE;
+      if (l < gs_n_light<S>(g)) {
+        const bool src = gs_src<S>(g, l);
         float Xb, Yb;
-        gen_light_reverse(g.light[l], l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y, gimg,
-                          acc + G_LIGHT + 10 * l, Xb, Yb);
+        if constexpr (S::kStatic)
+          gen_light_reverse_body(g.light[l], S::light(l), l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y,
+                                 gimg, acc + G_LIGHT + 10 * l, Xb, Yb);
+        else
+          gen_light_reverse(g.light[l], l, st, g.shp_tab, src ? bx : xy.x, src ? by : xy.y, gimg,
+                            acc + G_LIGHT + 10 * l, Xb, Yb);
         if (src) {
           bxb += Xb;
           byb += Yb;
         }
       }
     const float abx = -bxb, aby = -byb;   // beta = theta - sum alpha
-    if (g.has_shear) {
+    if (has_shear) {
       acc[G_SH] += abx * xy.x - aby * xy.y;
       acc[G_SH + 1] += abx * xy.y + aby * xy.x;
     }
 #pragma unroll
     for (int s = 0; s < kGenMass; ++s)
-      if (s < g.n_mass) {
-        if (g.mass[s].type == GL_PROF_EPL)
+      if (s < gs_n_mass<S>(g)) {
+        if (gs_mass<S>(g, s) == GL_PROF_EPL)
           epl_backprop(ec, es, abx, aby, ea);
+        else if constexpr (S::kStatic)
+          gen_mass_reverse_body(g.mass[s], S::mass(s), s, st, xy.x, xy.y, abx, aby, acc + G_MASS + 8 * s);
         else
-          gen_mass_reverse(g.mass[s], st.x, xy.x, xy.y, abx, aby, acc + G_MASS + 8 * s);
+          gen_mass_reverse(g.mass[s], s, st, xy.x, xy.y, abx, aby, acc + G_MASS + 8 * s);
       }
     }   // !isnan(img)
     }   // px < total
@@ -953,7 +1047,7 @@ static __device__ void phase_pixels_reverse_gen(const FusedArgs& a, const DevIma
   // the EPL slot's accumulators
 #pragma unroll
   for (int s = 0; s < kGenMass; ++s)
-    if (s < g.n_mass && g.mass[s].type == GL_PROF_EPL) {
+    if (s < gs_n_mass<S>(g) && gs_mass<S>(g, s) == GL_PROF_EPL) {
       float* e = acc + G_MASS + 8 * s;
       e[0] = ea.phi; e[1] = ea.SP; e[2] = ea.SPlnR; e[3] = ea.FH;
       e[4] = ea.FT; e[5] = ea.q; e[6] = ea.cx; e[7] = ea.cy;
@@ -994,6 +1088,10 @@ static __device__ void sample_chain_gen(const FusedArgs& a, SmemStatic& st, int 
       epl_chain(pget(sx, m.col[0], 0.f), pget(sx, m.col[1], 2.f), pget(sx, m.col[2], 0.f),
                 pget(sx, m.col[3], 0.f), ec, ea, gr);
       scatter(st.gx, m.col, gr, 6);
+    } else if (m.type == GL_PROF_SIE) {
+      float gr[5];
+      sie_chain(pget(sx, m.col[0], 0.f), pget(sx, m.col[1], 0.f), pget(sx, m.col[2], 0.f), e, gr);
+      scatter(st.gx, m.col, gr, 5);
     } else {
       const int np = m.type == GL_PROF_SIS ? 3 : 5;
       scatter(st.gx, m.col, e, np);
@@ -1087,7 +1185,7 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
   const int tid = threadIdx.x;
 
   compute_term_counts(a, st);
-  if (FAM == FAM_GENERIC && tid <= kMaxShapeletN) {
+  if (kGenFamily<FAM> && tid <= kMaxShapeletN) {
     double f = 1.0;
     for (int i = 2; i <= tid; ++i) f *= i;
     st.pref[tid] = (float)(1.0 / sqrt(pow(2.0, (double)tid) * sqrt(3.14159265358979323846) * f));
@@ -1119,10 +1217,18 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
         st.x[tid] = v;
       }
     }
-    if (FAM == FAM_GENERIC && a.gen.amps && tid < a.gen.n_amp)
+    if (kGenFamily<FAM> && a.gen.amps && tid < a.gen.n_amp)
       st.amp[tid] = a.gen.amps[(size_t)b * a.gen.n_amp + tid];
     __syncthreads();
-    if (FAM == FAM_GENERIC && tid >= 32 && tid < 32 + a.gen.n_light) {
+    if (kGenFamily<FAM> && tid >= 64 && tid < 64 + a.gen.n_mass) {
+      // SIE constants of the general path's mass slots
+      const DevProfile& m = a.gen.mass[tid - 64];
+      if (m.type == GL_PROF_SIE)
+        st.gsie[tid - 64] = sie_consts(pget(st.x, m.col[0], 0.f), pget(st.x, m.col[1], 0.f),
+                                       pget(st.x, m.col[2], 0.f), pget(st.x, m.col[3], 0.f),
+                                       pget(st.x, m.col[4], 0.f));
+    }
+    if (kGenFamily<FAM> && tid >= 32 && tid < 32 + a.gen.n_light) {
       // Sersic constants of the general path's light slots
       const GenLight& L = a.gen.light[tid - 32];
       if (L.type == GL_PROF_SERSIC_ELLIPSE) {
@@ -1142,16 +1248,16 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
     }
     __syncthreads();
 
-    if constexpr (FAM == FAM_GENERIC)
-      phase_pixels_forward_gen(a, I, sm, st, K);
+    if constexpr (kGenFamily<FAM>)
+      phase_pixels_forward_gen<GenSig<FAM>>(a, I, sm, st, K);
     else
       phase_pixels_forward<FAM>(a, I, sm, st, K);
     __syncthreads();
 
     float lsum = 0.f, csum = 0.f;
     float* img_out = a.img_out ? a.img_out + (size_t)b * a.img_stride : nullptr;
-    const float* err_map = (FAM == FAM_GENERIC && a.gen.noise_err) ? I.err : nullptr;
-    const float cf = (FAM == FAM_GENERIC && a.gen.unit_cf) ? 1.f : I.cf;
+    const float* err_map = (kGenFamily<FAM> && a.gen.noise_err) ? I.err : nullptr;
+    const float cf = (kGenFamily<FAM> && a.gen.unit_cf) ? 1.f : I.cf;
 #define GL_CALL_FWD(KSV) \
   phase_conv_forward<KSV, X2>(I, sm, img_out, a.want_grad != 0, err_map, cf, lsum, csum)
     GL_KS_DISPATCH(I.KS, GL_CALL_FWD)
@@ -1169,8 +1275,8 @@ __global__ void __launch_bounds__(kThreads, 1) fused_kernel(const __grid_constan
       GL_KS_DISPATCH(I.KS, GL_CALL_ADJ)
 #undef GL_CALL_ADJ
       __syncthreads();
-      if constexpr (FAM == FAM_GENERIC) {
-        phase_pixels_reverse_gen(a, I, sm, st, K);
+      if constexpr (kGenFamily<FAM>) {
+        phase_pixels_reverse_gen<GenSig<FAM>>(a, I, sm, st, K);
         if (tid == 0) sample_chain_gen(a, st, K);
       } else {
         phase_pixels_reverse<FAM>(a, I, sm, st, K);

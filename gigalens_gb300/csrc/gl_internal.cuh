@@ -75,8 +75,14 @@ enum ModelFamily : int {
   FAM_EPL_SE_SE = 2,        // EPL         ; SersicEllipse            ; SersicEllipse
   FAM_EPL_SE = 3,           // EPL         ; no lens light            ; SersicEllipse
   FAM_GENERIC = 4,          // general path: the profile lists of GenArgs, dispatched per pixel
-  FAM_COUNT = 5
+  // general path compiled for one model signature (profile code inlined)
+  FAM_SIG_SIE_SHEAR_SE_SE = 5,   // SIE + Shear ; SersicEllipse ; SersicEllipse
+  FAM_SIG_SIS_SHEAR_SE_SE = 6,   // SIS + Shear ; SersicEllipse ; SersicEllipse
+  FAM_SIG_EPL_SHEAR_SHP = 7,     // EPL + Shear ; no lens light ; Shapelets (BackwardProbModel gradient)
+  FAM_COUNT = 8
 };
+// Families that run the general path's code (FusedArgs::gen describes the model).
+inline bool is_gen_family(int fam) { return fam >= FAM_GENERIC; }
 
 // A light profile of the general path.
 struct GenLight {
@@ -152,6 +158,7 @@ struct gl_plan {
   gl::DevProfile epl, shear, llight, source;
   gl::GenArgs gen;          // the model on the fused kernel's general path
   int gen_ok;               // gen describes the model
+  int gen_family;           // FAM_GENERIC or the compiled signature that matches gen
   int fused_fits;           // the images fit the fused kernel's shared memory
   float* gscratch;          // otherwise: per-CTA plane storage in global memory
   int cta_floats;           // floats per CTA in gscratch

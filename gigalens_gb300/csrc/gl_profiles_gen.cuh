@@ -62,6 +62,88 @@ __device__ __forceinline__ void sie_alpha_t(const T& theta_E, const T& e1, const
   ay = fx * sp + fy * cp;
 }
 
+// SIE on the fused kernel's general path: the per-sample constants once
+// (the same operations as sie_alpha_t), the deflection per pixel, and a
+// hand-written reverse mode that accumulates the adjoints of the per-sample
+// intermediates B = b / sqrt(1 - q^2), sq = sqrt(1 - q^2), q^2, phi and the
+// centre; sie_chain maps them to (theta_E, e1, e2, center_x, center_y) once
+// per sample.
+struct SieC {
+  float B, sq, q2, cp, sp, cx, cy;
+};
+__device__ __forceinline__ SieC sie_consts(float theta_E, float e1, float e2, float cx, float cy) {
+  const float phi = atan2f(e2, e1) * 0.5f;
+  float c = sqrtf(e1 * e1 + e2 * e2);
+  if (c > 0.9999f) c = 0.9999f;
+  const float q = (1.f - c) / (1.f + c);
+  const float q2 = q * q;
+  const float theta_E_conv = theta_E / sqrtf((1.f + q2) / (2.f * q));
+  const float b = theta_E_conv * sqrtf((1.f + q2) / 2.f);
+  SieC k;
+  k.sq = sqrtf(1.f - q2);
+  k.B = b / k.sq;
+  k.q2 = q2;
+  k.cp = cosf(phi);
+  k.sp = sinf(phi);
+  k.cx = cx;
+  k.cy = cy;
+  return k;
+}
+__device__ __forceinline__ void sie_alpha(const SieC& k, float x, float y, float& ax, float& ay) {
+  const float dx = x - k.cx, dy = y - k.cy;
+  const float xr = dx * k.cp + dy * k.sp;
+  const float yr = -dx * k.sp + dy * k.cp;
+  const float psi = sqrtf(k.q2 * (xr * xr) + yr * yr);
+  const float fx = k.B * atanf(k.sq * xr / psi);
+  const float fy = k.B * atanhf(k.sq * yr / psi);
+  ax = fx * k.cp - fy * k.sp;
+  ay = fx * k.sp + fy * k.cp;
+}
+// Adjoint slots: 0 B, 1 sq, 2 q^2, 3 phi, 4 center_x, 5 center_y.
+constexpr int kSieAcc = 6;
+__device__ __forceinline__ void sie_backprop(const SieC& k, float x, float y, float abx, float aby, float* acc) {
+  const float dx = x - k.cx, dy = y - k.cy;
+  const float xr = dx * k.cp + dy * k.sp;
+  const float yr = -dx * k.sp + dy * k.cp;
+  const float ipsi = 1.f / sqrtf(k.q2 * (xr * xr) + yr * yr);
+  const float u = k.sq * xr * ipsi, v = k.sq * yr * ipsi;
+  const float au = atanf(u), av = atanhf(v);
+  const float fx = k.B * au, fy = k.B * av;
+  // alpha = R(-phi) (fx, fy): the rotation's phi adjoint, then (fx, fy)
+  acc[3] += abx * (-fx * k.sp - fy * k.cp) + aby * (fx * k.cp - fy * k.sp);
+  const float fxb = abx * k.cp + aby * k.sp, fyb = -abx * k.sp + aby * k.cp;
+  acc[0] += fxb * au + fyb * av;
+  const float ub = fxb * k.B / (1.f + u * u), vb = fyb * k.B / (1.f - v * v);
+  acc[1] += (ub * xr + vb * yr) * ipsi;
+  // u = sq xr / psi, v = sq yr / psi, psi^2 = q^2 xr^2 + yr^2
+  const float psib = -(ub * u + vb * v) * ipsi;
+  acc[2] += psib * 0.5f * xr * xr * ipsi;
+  const float xrb = (ub * k.sq + psib * k.q2 * xr) * ipsi;
+  const float yrb = (vb * k.sq + psib * yr) * ipsi;
+  // (xr, yr) = R(phi) (dx, dy)
+  acc[3] += xrb * yr - yrb * xr;
+  acc[4] -= xrb * k.cp - yrb * k.sp;
+  acc[5] -= xrb * k.sp + yrb * k.cp;
+}
+// d logL / d(theta_E, e1, e2, center_x, center_y) from the adjoints (thread 0).
+__device__ __forceinline__ void sie_chain(float theta_E, float e1, float e2, const float* acc, float out[5]) {
+  using D3 = Dual<3>;
+  const D3 tE = D3::seed(theta_E, 0), E1 = D3::seed(e1, 1), E2 = D3::seed(e2, 2);
+  const D3 phi = gatan2(E2, E1) * 0.5f;
+  D3 c = gsqrt0(E1 * E1 + E2 * E2);
+  if (val(c) > 0.9999f) c = D3(0.9999f);
+  const D3 q = (1.f - c) / (1.f + c);
+  const D3 q2 = q * q;
+  const D3 theta_E_conv = tE / gsqrt((1.f + q2) / (2.f * q));
+  const D3 b = theta_E_conv * gsqrt((1.f + q2) / 2.f);
+  const D3 sq = gsqrt(1.f - q2);
+  const D3 B = b / sq;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) out[i] = acc[0] * B.d[i] + acc[1] * sq.d[i] + acc[2] * q2.d[i] + acc[3] * phi.d[i];
+  out[3] = acc[4];
+  out[4] = acc[5];
+}
+
 // ------------------------------------------------------------------ TNFW
 // F(x) of the NFW profile, tnfw.py:41-58 (exactly 1 at x == 1)
 template <class T>

@@ -81,13 +81,17 @@ extern "C" {
  * The fused kernel has compiled fast paths for EPL [+ SHEAR] with
  * SERSIC / SERSIC_ELLIPSE lens light and source; every other model with at
  * most 2 mass profiles besides SHEAR (at most one EPL), at most one SHEAR
- * and at most 3 light profiles runs on its general path.  Gradients with
- * respect to explicit shapelet amplitudes are computed for one shapelet
- * profile per model (more give GL_ERR_UNSUPPORTED).
+ * and at most 3 light profiles runs on its general path; three model
+ * signatures of the general path are compiled with their profile code
+ * inlined (SIE or SIS + SHEAR with SERSIC_ELLIPSE lens light and source;
+ * EPL + SHEAR with one SHAPELETS source, explicit or solved linearly).
+ * Gradients with respect to explicit shapelet amplitudes are computed for
+ * one shapelet profile per model (more give GL_ERR_UNSUPPORTED).
  * Images whose supersampled planes exceed a CTA's shared memory (about 90 x 90
- * at ss = 2 with a 41-pixel PSF), and every image on the general path, keep
- * them in a per-CTA slice of a global scratch owned by the plan: calls on one
- * such plan must not overlap on the GPU (one stream, or serialised).       */
+ * at ss = 2 with a 41-pixel PSF), and every image on the general path outside
+ * those signatures, keep them in a per-CTA slice of a global scratch owned by
+ * the plan: calls on one such plan must not overlap on the GPU (one stream,
+ * or serialised).                                                          */
 typedef struct {
   int type;                        /* GL_PROF_*                            */
   int group;                       /* GL_GROUP_*                           */
@@ -282,7 +286,11 @@ typedef struct {
   int blocks;              /* CTAs of a launch of bs samples            */
   int samples_per_cta;     /* ceil(bs / blocks)                          */
   int smem_bytes;          /* dynamic shared memory per CTA             */
-  int family;              /* 0..3 compiled fast paths, 4 general path  */
+  int family;              /* 0..3 compiled fast paths, 4 general path,
+                              5..7 general path compiled for one model
+                              signature: 5 SIE + shear, 6 SIS + shear (each
+                              with SersicEllipse lens light and source),
+                              7 EPL + shear with a shapelet source          */
   int global_planes;       /* 1: the image planes live in global memory */
   int subkernel_side;      /* largest parity sub-kernel side            */
   int col_block;           /* correlation outputs per lane              */

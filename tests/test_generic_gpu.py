@@ -56,6 +56,21 @@ def _model(name):
                 Ie=tfd.LogNormal(math.log(200.0), 0.3)))]),
             tfd.JointDistributionSequential([_se_prior(0.25, 150.0, 0.2)]),
         ])
+    elif name in ("sie_shear_se_se", "sis_shear_se_se"):
+        # compiled signatures of the general path (family 5: SIE, 6: SIS)
+        mass = sie.SIE() if name.startswith("sie") else sis.SIS()
+        phys = PhysicalModel([mass, shear.Shear()], [sersic.SersicEllipse()], [sersic.SersicEllipse()])
+        om = dict(lenses=[(name[:3].upper(), {}), ("SHEAR", {})], lens_light=[("SERSIC_ELLIPSE", {})],
+                  source_light=[("SERSIC_ELLIPSE", {})])
+        lens = dict(theta_E=tfd.LogNormal(math.log(1.2), 0.1), center_x=tfd.Normal(0, 0.05),
+                    center_y=tfd.Normal(0, 0.05))
+        if name.startswith("sie"):
+            lens.update(e1=tfd.Normal(0, 0.1), e2=tfd.Normal(0, 0.1))
+        prior = tfd.JointDistributionSequential([
+            tfd.JointDistributionSequential([tfd.JointDistributionNamed(lens), _shear_prior()]),
+            tfd.JointDistributionSequential([_se_prior(1.0, 300.0)]),
+            tfd.JointDistributionSequential([_se_prior(0.25, 150.0, 0.2)]),
+        ])
     elif name == "epl_tnfw_shear_se":
         phys = PhysicalModel([epl.EPL(50), tnfw.TNFW(), shear.Shear()], [], [sersic.SersicEllipse()])
         om = dict(lenses=[("EPL", {"niter": 50}), ("TNFW", {}), ("SHEAR", {})], lens_light=[],
@@ -141,8 +156,18 @@ IMAGE_LIMITS = {
     "sis_shapelets_interp": dict(band_fraction=1e-2, max_rel=5e-4),
 }
 
+# Largest relative gradient error allowed where the float32 restatement's own
+# noise band exceeds the default 1e-2: in sis_shear_se_se one sample's shear
+# gradient is a sum over pixels that cancels (measured band 1.32e-2 of the
+# component's scale, kernel error 1.13e-2, inside twice the band).
+GRAD_LIMITS = {"sis_shear_se_se": 2e-2}
+
 GRAD_CASES = ["sie_shear_coresersic_se", "epl_tnfw_shear_se", "sis_se_two_sources", "sis_shapelets_explicit",
-              "sis_shapelets_interp"]
+              "sis_shapelets_interp", "sie_shear_se_se", "sis_shear_se_se"]
+# the model family each case's plan must take (4: run-time general path; 5, 6:
+# the compiled SIE / SIS + shear signatures)
+CASE_FAMILY = {"sie_shear_se_se": 5, "sis_shear_se_se": 6, "sie_shear_coresersic_se": 4, "epl_tnfw_shear_se": 4,
+               "sis_se_two_sources": 4, "sis_shapelets_explicit": 4, "sis_shapelets_interp": 4}
 
 
 @pytest.mark.parametrize("name", GRAD_CASES)
@@ -161,6 +186,10 @@ def test_general_path_loglik_grad(name):
     plan = s["sim"].prob_plan(s["pm"])
     x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
     bs = x.shape[0]
+    cfg = plan.launch_config(bs)
+    assert cfg["family"] == CASE_FAMILY[name]
+    # the compiled signatures keep 40x40 px planes in shared memory
+    assert cfg["global_planes"] == (1 if CASE_FAMILY[name] == 4 else 0)
     logL = torch.empty(bs, device="cuda")
     chi2 = torch.empty(bs, device="cuda")
     grad = torch.empty_like(x)
@@ -174,7 +203,7 @@ def test_general_path_loglik_grad(name):
                                                               dtype=torch.float32)[0], x.cpu(), g)
     _check_scalar(logL, ll.detach(), 1e-4, name="logL")
     _check_scalar(chi2, c2.detach(), 1e-4, name="chi2")
-    _check_grad(grad, (g, band))
+    _check_grad(grad, (g, band), max_rel=GRAD_LIMITS.get(name, 1e-2))
 
 
 def test_general_path_log_prob_autograd():
@@ -274,28 +303,32 @@ def test_profile_eval_new_types(kind):
 
 
 # ------------------------------------------------------------- least-squares gradient
-def _lsq_setup(bs=5, num_pix=40, n_max=3, seed=0):
+def _lsq_setup(bs=5, num_pix=40, n_max=3, seed=0, lens_light=True):
+    """The BackwardProbModel case: EPL + shear, shapelet source (and a Sersic
+    lens light, both solved linearly).  Without the lens light the model is
+    the compiled EPL + shear + shapelets signature of the general path."""
     from gigalens_gb300.cuda.profiles.light import sersic, shapelets
     from gigalens_gb300.cuda.profiles.mass import epl, shear
 
-    phys = PhysicalModel([epl.EPL(50), shear.Shear()], [sersic.SersicEllipse(use_lstsq=True)],
+    phys = PhysicalModel([epl.EPL(50), shear.Shear()], [sersic.SersicEllipse(use_lstsq=True)] if lens_light else [],
                          [shapelets.Shapelets(n_max, use_lstsq=True, interpolate=False)])
-    om = dict(lenses=[("EPL", {"niter": 50}), ("SHEAR", {})], lens_light=[("SERSIC_ELLIPSE", {})],
+    om = dict(lenses=[("EPL", {"niter": 50}), ("SHEAR", {})],
+              lens_light=[("SERSIC_ELLIPSE", {})] if lens_light else [],
               source_light=[("SHAPELETS", {"n_max": n_max})])
-    prior = tfd.JointDistributionSequential([
-        tfd.JointDistributionSequential([
-            tfd.JointDistributionNamed(dict(theta_E=tfd.LogNormal(math.log(1.25), 0.1),
-                                            gamma=tfd.TruncatedNormal(2, 0.1, 1.6, 2.4),
-                                            e1=tfd.Normal(0, 0.1), e2=tfd.Normal(0, 0.1),
-                                            center_x=tfd.Normal(0, 0.05), center_y=tfd.Normal(0, 0.05))),
-            _shear_prior()]),
-        tfd.JointDistributionSequential([tfd.JointDistributionNamed(dict(
+    groups = [tfd.JointDistributionSequential([
+        tfd.JointDistributionNamed(dict(theta_E=tfd.LogNormal(math.log(1.25), 0.1),
+                                        gamma=tfd.TruncatedNormal(2, 0.1, 1.6, 2.4),
+                                        e1=tfd.Normal(0, 0.1), e2=tfd.Normal(0, 0.1),
+                                        center_x=tfd.Normal(0, 0.05), center_y=tfd.Normal(0, 0.05))),
+        _shear_prior()])]
+    if lens_light:
+        groups.append(tfd.JointDistributionSequential([tfd.JointDistributionNamed(dict(
             R_sersic=tfd.LogNormal(math.log(1.0), 0.15), n_sersic=tfd.Uniform(2, 4),
             e1=tfd.TruncatedNormal(0, 0.1, -0.3, 0.3), e2=tfd.TruncatedNormal(0, 0.1, -0.3, 0.3),
-            center_x=tfd.Normal(0, 0.05), center_y=tfd.Normal(0, 0.05)))]),
-        tfd.JointDistributionSequential([tfd.JointDistributionNamed(dict(
-            beta=tfd.LogNormal(math.log(0.12), 0.1), center_x=tfd.Normal(0, 0.1), center_y=tfd.Normal(0, 0.1)))]),
-    ])
+            center_x=tfd.Normal(0, 0.05), center_y=tfd.Normal(0, 0.05)))]))
+    groups.append(tfd.JointDistributionSequential([tfd.JointDistributionNamed(dict(
+        beta=tfd.LogNormal(math.log(0.12), 0.1), center_x=tfd.Normal(0, 0.1), center_y=tfd.Normal(0, 0.1)))]))
+    prior = tfd.JointDistributionSequential(groups)
     ksub = gaussian_psf(0.1, 0.0325, 13)
     cfg = SimulatorConfig(delta_pix=0.065, num_pix=num_pix, supersample=2, kernel_supersampled=ksub)
     ocfg = O.SimConfig(0.065, num_pix, 2, ksub.astype(np.float64))
@@ -321,13 +354,14 @@ def _oracle_backward(s, x, dtype=torch.float64):
     return O.backward_log_likelihood(im, s["obs"].astype(npd), s["err"].astype(npd))
 
 
-@pytest.mark.parametrize("num_pix", [40, 100])
-def test_lstsq_grad_matches_oracle_through_pinv(num_pix):
+@pytest.mark.parametrize("num_pix,lens_light", [(40, True), (100, True), (40, False), (100, False)])
+def test_lstsq_grad_matches_oracle_through_pinv(num_pix, lens_light):
     """gl_lstsq_grad (envelope theorem at the solved coefficients) against the
     float64 oracle differentiated through pinv, as TensorFlow differentiates
     tf/model.py:152-158.  100 px planes exceed shared memory and run from
-    global memory."""
-    s = _lsq_setup(num_pix=num_pix, bs=5 if num_pix < 64 else 3)
+    global memory.  Without lens light the model is the compiled EPL + shear +
+    shapelets signature; with it, the run-time general path."""
+    s = _lsq_setup(num_pix=num_pix, bs=5 if num_pix < 64 else 3, lens_light=lens_light)
     plan = s["sim"].lstsq_plan(s["obs"], s["err"])
     x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
     r = s["sim"].run_lstsq(plan, x, want_image=False, want_loglik=True)
