@@ -9,15 +9,16 @@
 // streamed from HBM in chunks of 64 through a ring of chunks in shared memory
 // (cp.async; each thread copies and later converts the same 16-byte pieces,
 // with its own copy of their weights, so it only waits for its own copy
-// groups).  A chunk is weighted, split into
+// groups; up to seven chunks of copies in flight per SM hide the HBM
+// latency).  A chunk is weighted, split into
 // TF32 head and tail (3xTF32: a_i a_j ~ hi_i hi_j + hi_i lo_j + lo_i hi_j,
 // FP32-level accuracy) and stored in the canonical K-major layout (8-row x
 // 16-byte core matrices; a K stride of 144 bytes keeps the 16-byte stores
 // conflict-free) as ONE 128-row operand: rows 0-63 hold the heads, rows 64-127
 // the tails.  With the heads as the B operand (N = R rounded up to 16), one
 // tcgen05.mma.kind::tf32 (M = 128, K = 8) gives HH = hi hi^T in TMEM lanes
-// 0-63 and LH = lo hi^T in lanes 64-127, and G = HH + LH + LH^T.  Four operand
-// stages keep the MMAs of three chunks in flight while the next is filled.
+// 0-63 and LH = lo hi^T in lanes 64-127, and G = HH + LH + LH^T.  Two operand
+// stages keep one chunk's MMAs in flight while the next is filled.
 // Every 1024 pixels the accumulation switches between two TMEM accumulators;
 // the finished one is read back (tcgen05.ld) one segment later, when its MMAs
 // are long complete, and added into float-float (TwoSum) sums of the lower
@@ -42,13 +43,13 @@ constexpr int kRmax = 64;
 constexpr uint32_t kLBO = 144;             // bytes between K-adjacent core matrices
 constexpr uint32_t kSBO = kLBO * kQ;       // bytes between row groups (8 rows)
 constexpr int kTileBytes = (kM / 8) * kSBO;   // one operand stage
-constexpr int kStages = 4;                 // operand stages
+constexpr int kStages = 2;                 // operand stages (the MMAs of one chunk take ~200 cycles)
 constexpr int kRowBytes = kKC * 4;         // one row of a raw chunk
 constexpr int kSegChunks = 16;             // chunks per TMEM accumulation segment (1024 px)
 constexpr uint32_t kTmemCols = 128;        // two accumulators of 64 columns
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr int kCtrlBytes = 1024;
-constexpr int kMaxRing = 6, kMinRing = 2;
+constexpr int kMaxRing = 8, kMinRing = 2;   // ring slots: up to 7 chunks in flight per SM
 constexpr int kSmemLimit = 227 * 1024;
 
 __host__ __device__ constexpr int tri_entries(int R) { return R * (R + 1) / 2; }
@@ -76,7 +77,9 @@ __device__ __forceinline__ void cp_wait_ring(int depth) {
     case 3: cp_async_wait<2>(); break;
     case 4: cp_async_wait<3>(); break;
     case 5: cp_async_wait<4>(); break;
-    default: cp_async_wait<5>(); break;
+    case 6: cp_async_wait<5>(); break;
+    case 7: cp_async_wait<6>(); break;
+    default: cp_async_wait<7>(); break;
   }
 }
 

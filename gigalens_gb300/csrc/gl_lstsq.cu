@@ -75,7 +75,6 @@ __device__ __forceinline__ void hermite_fn_n(int n, const float (&u)[U], float (
   for (int k = 0; k < U; ++k) out[k] = h1[k] * pref[n];
 }
 
-constexpr int kEvalU = 4;   // pixels per thread and iteration in the channel evaluation
 
 struct LsqShared {
   float x[GL_MAX_PARAMS];
@@ -156,6 +155,131 @@ __device__ void lsq_pass_conv(const LsqImage& I, const float* sm, int c0, int nb
   }
 }
 
+// Channel evaluation loop over the pixels 0 <= i < per_plane of a plane set
+// (i = (plane row - Ya) * N + column, the band's in-image rows from Ya) by
+// NTH threads: a thread takes U2 positions i per step and at each position
+// the pixel of every one of the NPL parity planes (NPL = ss^2; one index
+// division for NPL pixels), so U2 * NPL evaluations and their coordinate
+// loads interleave.  val(px, py, v) computes the basis values from their
+// coordinates; NaN values are stored as 0 (the reference zeroes NaN pixels).
+template <int NTH, int NPL, int U2, class Val>
+__device__ __forceinline__ void lsq_eval_loop(const LsqImage& I, float* sbase, const float2* bp,
+                                              const float4* gp, bool src, int per_plane, Val&& val) {
+  constexpr int U = NPL * U2;
+  const float inv_n = 1.f / (float)I.N;
+  const size_t gstride = (size_t)I.N * I.N;   // the grid holds whole-image planes
+  float* pb[NPL];                             // plane origins (column parity q = pq % ss)
+#pragma unroll
+  for (int pq = 0; pq < NPL; ++pq) pb[pq] = sbase + pq * I.plane_floats + I.padI[NPL == 4 ? (pq & 1) : 0];
+  for (int i0 = threadIdx.x; i0 < per_plane; i0 += U2 * NTH) {
+    float px[U], py[U];
+#pragma unroll
+    for (int m = 0; m < U2; ++m) {
+      const int i = min(i0 + m * NTH, per_plane - 1);
+#pragma unroll
+      for (int pq = 0; pq < NPL; ++pq) {
+        if (src) {
+          const float2 bt = bp[(size_t)pq * per_plane + i];
+          px[m * NPL + pq] = bt.x;
+          py[m * NPL + pq] = bt.y;
+        } else {
+          const float4 xy = __ldg(gp + pq * gstride + i);
+          px[m * NPL + pq] = xy.x;
+          py[m * NPL + pq] = xy.y;
+        }
+      }
+    }
+    float v[U];
+    val(px, py, v);
+#pragma unroll
+    for (int m = 0; m < U2; ++m) {
+      const int i = i0 + m * NTH;
+      if (i < per_plane) {
+        const int r = small_div(i, inv_n);
+        const int off = r * I.pitch + (i - r * I.N);
+#pragma unroll
+        for (int pq = 0; pq < NPL; ++pq) {
+          float x = v[m * NPL + pq];
+          if (isnan(x)) x = 0.f;
+          pb[pq][off] = x;
+        }
+      }
+    }
+  }
+}
+
+// Basis values of one channel (see lsq_eval_loop).
+template <int NTH, int NPL, int U2>
+__device__ __forceinline__ void lsq_eval_channel(const LsqArgs& a, const LsqImage& I, const float* sx,
+                                                 const float* pref, float* sbase, const float2* bp,
+                                                 const float4* gp, const LsqChannel& ch, int per_plane) {
+  constexpr int U = NPL * U2;
+  const LsqProfile& pr = a.prof[ch.prof];
+  const bool src = pr.group == GL_GROUP_SOURCE;
+  if (ch.kind == 1 && pr.interp) {   // tabulated shapelet functions (interpolate=True)
+    const float beta_s = lpget(sx, pr.col[0], 1.f);
+    const float cx = lpget(sx, pr.col[1], 0.f), cy = lpget(sx, pr.col[2], 0.f);
+    const float* tab = a.shp_tab;
+    const int n1 = ch.n1, n2 = ch.n2;
+    lsq_eval_loop<NTH, NPL, U2>(I, sbase, bp, gp, src, per_plane,
+                                [=](const float (&px)[U], const float (&py)[U], float (&v)[U]) {
+#pragma unroll
+                                  for (int k = 0; k < U; ++k) {
+                                    const float u = (px[k] - cx) / beta_s, w = (py[k] - cy) / beta_s;
+                                    v[k] = shp_tab_value(tab, n1, shp_lerp(u)) * shp_tab_value(tab, n2, shp_lerp(w));
+                                  }
+                                });
+  } else if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
+    const float ib = 1.f / lpget(sx, pr.col[0], 1.f);
+    const float cx = lpget(sx, pr.col[1], 0.f), cy = lpget(sx, pr.col[2], 0.f);
+    const int n1 = ch.n1, n2 = ch.n2;
+    lsq_eval_loop<NTH, NPL, U2>(I, sbase, bp, gp, src, per_plane,
+                                [=](const float (&px)[U], const float (&py)[U], float (&v)[U]) {
+                                  float u[U], w[U], hu[U], hw[U];
+#pragma unroll
+                                  for (int k = 0; k < U; ++k) {
+                                    u[k] = (px[k] - cx) * ib;
+                                    w[k] = (py[k] - cy) * ib;
+                                  }
+                                  hermite_fn_n<U>(n1, u, hu, pref);
+                                  hermite_fn_n<U>(n2, w, hw, pref);
+#pragma unroll
+                                  for (int k = 0; k < U; ++k) {
+                                    const float fac = expf(-(u[k] * u[k] + w[k] * w[k]) / 2.f);
+                                    v[k] = fac * hu[k] * hw[k];
+                                  }
+                                });
+  } else {              // unit-amplitude Sersic
+    const SerC sc = sersic_consts(lpget(sx, pr.col[0], 1.f), lpget(sx, pr.col[1], 1.f),
+                                  lpget(sx, pr.col[2], 0.f), lpget(sx, pr.col[3], 0.f),
+                                  lpget(sx, pr.col[4], 0.f), lpget(sx, pr.col[5], 0.f), 1.f);
+    lsq_eval_loop<NTH, NPL, U2>(I, sbase, bp, gp, src, per_plane,
+                                [=](const float (&px)[U], const float (&py)[U], float (&v)[U]) {
+#pragma unroll
+                                  for (int k = 0; k < U; ++k) v[k] = sersic_light(sc, px[k], py[k]);
+                                });
+  }
+}
+
+// Channel evaluation: the basis images of channels c0 .. c0 + CPn - 1 (one
+// plane set per slot) on the band's in-image rows Ya .. Ya + per_plane / N - 1
+// (shared-memory row 0 is plane row Ybase).  Source channels read the
+// ray-traced coordinates beta, lens-light channels the image-plane grid.
+template <int NTH>
+__device__ __forceinline__ void lsq_eval(const LsqArgs& a, const LsqImage& I, const float* sx,
+                                         const float* pref, float* sm, const float2* beta,
+                                         const float4* grid, int c0, int Ya, int Ybase, int per_plane) {
+  const float4* gp = grid + (size_t)Ya * I.N;
+  for (int slot = 0; slot < I.CPn && c0 + slot < a.D; ++slot) {
+    const LsqChannel ch = a.ch[c0 + slot];
+    float* sbase = sm + (size_t)slot * I.nplanes * I.plane_floats + (Ya - Ybase) * I.pitch;
+    if (I.nplanes == 4)
+      lsq_eval_channel<NTH, 4, 2>(a, I, sx, pref, sbase, beta, gp, ch, per_plane);
+    else
+      lsq_eval_channel<NTH, 1, 8>(a, I, sx, pref, sbase, beta, gp, ch, per_plane);
+  }
+}
+
 // Column blocks of 20 for sub-kernels up to 15 taps (register budget), 16 otherwise.
 #define GL_LSQ_CONV(KSV)                                                     \
   do {                                                                       \
@@ -198,7 +322,6 @@ __global__ void __launch_bounds__(NT, 512 / NT) lsq_basis_kernel(const __grid_co
     const int Ya = max(0, Ybase), Yb = min(I.N, Ybase + I.brows);
     const int nrows = Yb - Ya;                          // plane rows inside the image
     const int per_plane = nrows * I.N;
-    const float inv_n = 1.f / (float)I.N;
     if (tid < a.d) st.x[tid] = a.x[(size_t)b * a.d + tid];
     // zero the planes (halo rows and columns stay zero), load the sub-kernels
     for (int i = tid; i < I.offK / 4; i += NT) smem_dyn[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -236,120 +359,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) lsq_basis_kernel(const __grid_co
     __syncthreads();
     float* Xb = a.X + (size_t)b * a.xstride;
     for (int c0 = 0; c0 < a.D; c0 += I.CPn) {
-      // evaluate channels c0 .. c0+CPn-1 on the band's rows inside the image
-      for (int slot = 0; slot < I.CPn && c0 + slot < a.D; ++slot) {
-        const LsqChannel ch = a.ch[c0 + slot];
-        const LsqProfile& pr = a.prof[ch.prof];
-        const bool src = pr.group == GL_GROUP_SOURCE;
-        float* sbase = sm + (size_t)slot * I.nplanes * I.plane_floats + (Ya - Ybase) * I.pitch;
-        for (int pq = 0; pq < I.nplanes; ++pq) {
-          const int q = pq - (pq / I.ss) * I.ss;
-          float* pbase = sbase + pq * I.plane_floats + I.padI[q];
-          const float2* bp = beta + (size_t)pq * per_plane;
-          const float4* gp = grid + ((size_t)pq * I.N + Ya) * I.N;
-          // kEvalU pixels per thread: their loads and recursions interleave
-          if (ch.kind == 1 && pr.interp) {   // tabulated shapelet functions (interpolate=True)
-            const float beta_s = lpget(st.x, pr.col[0], 1.f);
-            const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
-            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * NT) {
-              float u[kEvalU], w[kEvalU];
-#pragma unroll
-              for (int k = 0; k < kEvalU; ++k) {
-                const int i = min(i0 + k * NT, per_plane - 1);
-                float px, py;
-                if (src) {
-                  const float2 bt = bp[i];
-                  px = bt.x;
-                  py = bt.y;
-                } else {
-                  const float4 xy = __ldg(gp + i);
-                  px = xy.x;
-                  py = xy.y;
-                }
-                u[k] = (px - cx) / beta_s;
-                w[k] = (py - cy) / beta_s;
-              }
-#pragma unroll
-              for (int k = 0; k < kEvalU; ++k) {
-                const int i = i0 + k * NT;
-                if (i < per_plane) {
-                  float val = shp_tab_value(a.shp_tab, ch.n1, shp_lerp(u[k])) *
-                              shp_tab_value(a.shp_tab, ch.n2, shp_lerp(w[k]));
-                  if (isnan(val)) val = 0.f;
-                  const int r = small_div(i, inv_n);
-                  pbase[r * I.pitch + (i - r * I.N)] = val;
-                }
-              }
-            }
-          } else if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
-            const float ib = 1.f / lpget(st.x, pr.col[0], 1.f);
-            const float cx = lpget(st.x, pr.col[1], 0.f), cy = lpget(st.x, pr.col[2], 0.f);
-            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * NT) {
-              float u[kEvalU], w[kEvalU];
-#pragma unroll
-              for (int k = 0; k < kEvalU; ++k) {
-                const int i = min(i0 + k * NT, per_plane - 1);
-                float px, py;
-                if (src) {
-                  const float2 bt = bp[i];
-                  px = bt.x;
-                  py = bt.y;
-                } else {
-                  const float4 xy = __ldg(gp + i);
-                  px = xy.x;
-                  py = xy.y;
-                }
-                u[k] = (px - cx) * ib;
-                w[k] = (py - cy) * ib;
-              }
-              float hu[kEvalU], hw[kEvalU];
-              hermite_fn_n<kEvalU>(ch.n1, u, hu, pref);
-              hermite_fn_n<kEvalU>(ch.n2, w, hw, pref);
-#pragma unroll
-              for (int k = 0; k < kEvalU; ++k) {
-                const int i = i0 + k * NT;
-                if (i < per_plane) {
-                  const float fac = expf(-(u[k] * u[k] + w[k] * w[k]) / 2.f);
-                  float val = fac * hu[k] * hw[k];
-                  if (isnan(val)) val = 0.f;
-                  const int r = small_div(i, inv_n);
-                  pbase[r * I.pitch + (i - r * I.N)] = val;
-                }
-              }
-            }
-          } else {              // unit-amplitude Sersic
-            const SerC sc = sersic_consts(lpget(st.x, pr.col[0], 1.f), lpget(st.x, pr.col[1], 1.f),
-                                          lpget(st.x, pr.col[2], 0.f), lpget(st.x, pr.col[3], 0.f),
-                                          lpget(st.x, pr.col[4], 0.f), lpget(st.x, pr.col[5], 0.f), 1.f);
-            for (int i0 = tid; i0 < per_plane; i0 += kEvalU * NT) {
-              float px[kEvalU], py[kEvalU];
-#pragma unroll
-              for (int k = 0; k < kEvalU; ++k) {
-                const int i = min(i0 + k * NT, per_plane - 1);
-                if (src) {
-                  const float2 bt = bp[i];
-                  px[k] = bt.x;
-                  py[k] = bt.y;
-                } else {
-                  const float4 xy = __ldg(gp + i);
-                  px[k] = xy.x;
-                  py[k] = xy.y;
-                }
-              }
-#pragma unroll
-              for (int k = 0; k < kEvalU; ++k) {
-                const int i = i0 + k * NT;
-                if (i < per_plane) {
-                  float val = sersic_light(sc, px[k], py[k]);
-                  if (isnan(val)) val = 0.f;
-                  const int r = small_div(i, inv_n);
-                  pbase[r * I.pitch + (i - r * I.N)] = val;
-                }
-              }
-            }
-          }
-        }
-      }
+      lsq_eval<NT>(a, I, st.x, pref, sm, beta, grid, c0, Ya, Ybase, per_plane);
       __syncthreads();
       GL_KS_DISPATCH(I.KS, GL_LSQ_CONV)
       __syncthreads();
