@@ -162,9 +162,10 @@ __device__ void lsq_pass_conv(const LsqImage& I, const float* sm, int c0, int nb
 // division for NPL pixels), so U2 * NPL evaluations and their coordinate
 // loads interleave.  val(px, py, v) computes the basis values from their
 // coordinates; NaN values are stored as 0 (the reference zeroes NaN pixels).
-template <int NTH, int NPL, int U2, class Val>
+template <int NTH, int NPL, int U2, bool GF, class Val>
 __device__ __forceinline__ void lsq_eval_loop(const LsqImage& I, float* sbase, const float2* bp,
-                                              const float4* gp, bool src, int per_plane, Val&& val) {
+                                              const float4* gp, const float* gfp, bool src, int per_plane,
+                                              Val&& val) {
   constexpr int U = NPL * U2;
   const float inv_n = 1.f / (float)I.N;
   const size_t gstride = (size_t)I.N * I.N;   // the grid holds whole-image planes
@@ -172,12 +173,13 @@ __device__ __forceinline__ void lsq_eval_loop(const LsqImage& I, float* sbase, c
 #pragma unroll
   for (int pq = 0; pq < NPL; ++pq) pb[pq] = sbase + pq * I.plane_floats + I.padI[NPL == 4 ? (pq & 1) : 0];
   for (int i0 = threadIdx.x; i0 < per_plane; i0 += U2 * NTH) {
-    float px[U], py[U];
+    float px[U], py[U], gf[U];
 #pragma unroll
     for (int m = 0; m < U2; ++m) {
       const int i = min(i0 + m * NTH, per_plane - 1);
 #pragma unroll
       for (int pq = 0; pq < NPL; ++pq) {
+        if constexpr (GF) gf[m * NPL + pq] = gfp[(size_t)pq * per_plane + i];
         if (src) {
           const float2 bt = bp[(size_t)pq * per_plane + i];
           px[m * NPL + pq] = bt.x;
@@ -190,7 +192,7 @@ __device__ __forceinline__ void lsq_eval_loop(const LsqImage& I, float* sbase, c
       }
     }
     float v[U];
-    val(px, py, v);
+    val(px, py, gf, v);
 #pragma unroll
     for (int m = 0; m < U2; ++m) {
       const int i = i0 + m * NTH;
@@ -208,11 +210,34 @@ __device__ __forceinline__ void lsq_eval_loop(const LsqImage& I, float* sbase, c
   }
 }
 
+// Shapelet basis values phi_n1(u) phi_n2(w) exp(-(u^2 + w^2) / 2) of U
+// pixels; GF: the Gaussian factors gf were computed once per sample with the
+// same operations (lsq_basis_kernel's ray-trace pass).
+template <int U, bool GF>
+__device__ __forceinline__ void shapelet_vals(const float (&px)[U], const float (&py)[U], const float (&gf)[U],
+                                              float cx, float cy, float ib, int n1, int n2, const float* pref,
+                                              float (&v)[U]) {
+  float u[U], w[U], hu[U], hw[U];
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    u[k] = (px[k] - cx) * ib;
+    w[k] = (py[k] - cy) * ib;
+  }
+  hermite_fn_n<U>(n1, u, hu, pref);
+  hermite_fn_n<U>(n2, w, hw, pref);
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    const float fac = GF ? gf[k] : expf(-(u[k] * u[k] + w[k] * w[k]) / 2.f);
+    v[k] = fac * hu[k] * hw[k];
+  }
+}
+
 // Basis values of one channel (see lsq_eval_loop).
 template <int NTH, int NPL, int U2>
 __device__ __forceinline__ void lsq_eval_channel(const LsqArgs& a, const LsqImage& I, const float* sx,
                                                  const float* pref, float* sbase, const float2* bp,
-                                                 const float4* gp, const LsqChannel& ch, int per_plane) {
+                                                 const float4* gp, const float* gfp, const LsqChannel& ch,
+                                                 int per_plane) {
   constexpr int U = NPL * U2;
   const LsqProfile& pr = a.prof[ch.prof];
   const bool src = pr.group == GL_GROUP_SOURCE;
@@ -221,8 +246,8 @@ __device__ __forceinline__ void lsq_eval_channel(const LsqArgs& a, const LsqImag
     const float cx = lpget(sx, pr.col[1], 0.f), cy = lpget(sx, pr.col[2], 0.f);
     const float* tab = a.shp_tab;
     const int n1 = ch.n1, n2 = ch.n2;
-    lsq_eval_loop<NTH, NPL, U2>(I, sbase, bp, gp, src, per_plane,
-                                [=](const float (&px)[U], const float (&py)[U], float (&v)[U]) {
+    lsq_eval_loop<NTH, NPL, U2, false>(I, sbase, bp, gp, nullptr, src, per_plane,
+                                [=](const float (&px)[U], const float (&py)[U], const float (&gf)[U], float (&v)[U]) {
 #pragma unroll
                                   for (int k = 0; k < U; ++k) {
                                     const float u = (px[k] - cx) / beta_s, w = (py[k] - cy) / beta_s;
@@ -230,31 +255,24 @@ __device__ __forceinline__ void lsq_eval_channel(const LsqArgs& a, const LsqImag
                                   }
                                 });
   } else if (ch.kind == 1) {   // shapelet basis function (unit amplitude)
+    if (ch.prof != a.gfac_prof) gfp = nullptr;
     const float ib = 1.f / lpget(sx, pr.col[0], 1.f);
     const float cx = lpget(sx, pr.col[1], 0.f), cy = lpget(sx, pr.col[2], 0.f);
     const int n1 = ch.n1, n2 = ch.n2;
-    lsq_eval_loop<NTH, NPL, U2>(I, sbase, bp, gp, src, per_plane,
-                                [=](const float (&px)[U], const float (&py)[U], float (&v)[U]) {
-                                  float u[U], w[U], hu[U], hw[U];
-#pragma unroll
-                                  for (int k = 0; k < U; ++k) {
-                                    u[k] = (px[k] - cx) * ib;
-                                    w[k] = (py[k] - cy) * ib;
-                                  }
-                                  hermite_fn_n<U>(n1, u, hu, pref);
-                                  hermite_fn_n<U>(n2, w, hw, pref);
-#pragma unroll
-                                  for (int k = 0; k < U; ++k) {
-                                    const float fac = expf(-(u[k] * u[k] + w[k] * w[k]) / 2.f);
-                                    v[k] = fac * hu[k] * hw[k];
-                                  }
-                                });
+    if (gfp)
+      lsq_eval_loop<NTH, NPL, U2, true>(I, sbase, bp, gp, gfp, src, per_plane,
+                                        [=](const float (&px)[U], const float (&py)[U], const float (&gf)[U],
+                                            float (&v)[U]) { shapelet_vals<U, true>(px, py, gf, cx, cy, ib, n1, n2, pref, v); });
+    else
+      lsq_eval_loop<NTH, NPL, U2, false>(I, sbase, bp, gp, nullptr, src, per_plane,
+                                         [=](const float (&px)[U], const float (&py)[U], const float (&gf)[U],
+                                             float (&v)[U]) { shapelet_vals<U, false>(px, py, gf, cx, cy, ib, n1, n2, pref, v); });
   } else {              // unit-amplitude Sersic
     const SerC sc = sersic_consts(lpget(sx, pr.col[0], 1.f), lpget(sx, pr.col[1], 1.f),
                                   lpget(sx, pr.col[2], 0.f), lpget(sx, pr.col[3], 0.f),
                                   lpget(sx, pr.col[4], 0.f), lpget(sx, pr.col[5], 0.f), 1.f);
-    lsq_eval_loop<NTH, NPL, U2>(I, sbase, bp, gp, src, per_plane,
-                                [=](const float (&px)[U], const float (&py)[U], float (&v)[U]) {
+    lsq_eval_loop<NTH, NPL, U2, false>(I, sbase, bp, gp, nullptr, src, per_plane,
+                                [=](const float (&px)[U], const float (&py)[U], const float (&gf)[U], float (&v)[U]) {
 #pragma unroll
                                   for (int k = 0; k < U; ++k) v[k] = sersic_light(sc, px[k], py[k]);
                                 });
@@ -273,10 +291,12 @@ __device__ __forceinline__ void lsq_eval(const LsqArgs& a, const LsqImage& I, co
   for (int slot = 0; slot < I.CPn && c0 + slot < a.D; ++slot) {
     const LsqChannel ch = a.ch[c0 + slot];
     float* sbase = sm + (size_t)slot * I.nplanes * I.plane_floats + (Ya - Ybase) * I.pitch;
+    const float* gfp = a.gfac_prof >= 0 ? reinterpret_cast<const float*>(beta + (size_t)I.nplanes * per_plane)
+                                         : nullptr;
     if (I.nplanes == 4)
-      lsq_eval_channel<NTH, 4, 2>(a, I, sx, pref, sbase, beta, gp, ch, per_plane);
+      lsq_eval_channel<NTH, 4, 2>(a, I, sx, pref, sbase, beta, gp, gfp, ch, per_plane);
     else
-      lsq_eval_channel<NTH, 1, 8>(a, I, sx, pref, sbase, beta, gp, ch, per_plane);
+      lsq_eval_channel<NTH, 1, 8>(a, I, sx, pref, sbase, beta, gp, gfp, ch, per_plane);
   }
 }
 
@@ -340,6 +360,15 @@ __global__ void __launch_bounds__(NT, 512 / NT) lsq_basis_kernel(const __grid_co
                                  lpget(st.x, e[3], 0.f), lpget(st.x, e[4], 0.f), lpget(st.x, e[5], 0.f), K);
       const float g1 = a.has_shear ? lpget(st.x, a.shear.col[0], 0.f) : 0.f;
       const float g2 = a.has_shear ? lpget(st.x, a.shear.col[1], 0.f) : 0.f;
+      // the Gaussian of the source shapelet profile (its channels' common factor)
+      float gib = 0.f, gcx = 0.f, gcy = 0.f;
+      if (a.gfac_prof >= 0) {
+        const LsqProfile& gp = a.prof[a.gfac_prof];
+        gib = 1.f / lpget(st.x, gp.col[0], 1.f);
+        gcx = lpget(st.x, gp.col[1], 0.f);
+        gcy = lpget(st.x, gp.col[2], 0.f);
+      }
+      float* gf = reinterpret_cast<float*>(beta + (size_t)I.nplanes * per_plane);
       for (int pq = 0; pq < I.nplanes; ++pq) {
         const float4* gp = grid + ((size_t)pq * I.N + Ya) * I.N;
         float2* bp = beta + (size_t)pq * per_plane;
@@ -353,6 +382,10 @@ __global__ void __launch_bounds__(NT, 512 / NT) lsq_basis_kernel(const __grid_co
             bt.y = bt.y - (g2 * xy.x - g1 * xy.y);
           }
           bp[i] = bt;
+          if (a.gfac_prof >= 0) {
+            const float u = (bt.x - gcx) * gib, w = (bt.y - gcy) * gib;
+            gf[(size_t)pq * per_plane + i] = expf(-(u * u + w * w) / 2.f);
+          }
         }
       }
     }
@@ -828,7 +861,8 @@ int lsq_plan_layout(LsqPlan* L, const gl_plan* plan, int ctas_per_sm, int col_bl
       set_error("least squares: image %d too large (%d px)", i, F.N);
       return GL_ERR_UNSUPPORTED;
     }
-    const size_t beta_n = (size_t)F.nplanes * std::min(I.brows, F.N) * F.N;
+    size_t beta_n = (size_t)F.nplanes * std::min(I.brows, F.N) * F.N;
+    if (L->gfac_prof >= 0) beta_n += (beta_n + 1) / 2;   // and the Gaussian factors (floats)
     if (beta_n > beta_per_cta) beta_per_cta = beta_n;
     if (I.smem_floats * 4 > smem) smem = I.smem_floats * 4;
     if (F.N * F.N > maxP) maxP = F.N * F.N;
@@ -954,6 +988,12 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
     return GL_ERR_UNSUPPORTED;
   }
   L->D = D;
+  // the first source shapelet profile (Hermite functions): its Gaussian is
+  // computed once per pixel and sample in the ray-trace pass
+  L->gfac_prof = -1;
+  for (int i = 0; i < L->n_prof && L->gfac_prof < 0; ++i)
+    if (L->prof[i].type == GL_PROF_SHAPELETS && !L->prof[i].interp && L->prof[i].group == GL_GROUP_SOURCE)
+      L->gfac_prof = i;
   for (int i = 0; i < plan->n_images; ++i) {
     const DevImage& F = plan->img[i];
     LsqImage& I = L->img[i];
@@ -1063,6 +1103,7 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   a.shear = L->shear;
   a.shp_tab = plan->shp_tab;
   a.has_shear = L->has_shear;
+  a.gfac_prof = L->gfac_prof;
   for (int i = 0; i < plan->n_images; ++i) a.img[i] = L->img[i];
   a.x = x;
   a.img_id = img_id;

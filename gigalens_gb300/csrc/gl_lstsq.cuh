@@ -55,6 +55,8 @@ struct LsqArgs {
   float2* beta;         // ray-traced source-plane coordinates, one slice per CTA
   size_t beta_stride;   // float2 per slice
   const float* shp_tab; // shapelet table (interpolating shapelet profiles), or null
+  int gfac_prof;        // source shapelet profile whose Gaussian the ray-trace pass stores after
+                        // beta in each slice (floats, same pixel order), or -1
   LsqProfile prof[kMaxLsqProfiles];
   LsqChannel ch[kMaxLsqChannels];
   DevProfile epl, shear;
@@ -70,7 +72,8 @@ struct LsqPlan {
   int n_sm;             // CTAs of the basis kernel at most (ctas_per_sm per SM)
   int nt, ctas_per_sm;  // basis kernel: threads per CTA (512 or 256) and CTAs per SM
   int col_block;        // forced correlation column block (0: planner's choice)
-  size_t beta_per_cta;  // float2 of the largest band's ray-traced coordinates
+  size_t beta_per_cta;  // float2 of the largest band's ray-traced coordinates (and Gaussian factors)
+  int gfac_prof;        // see LsqArgs
   LsqProfile prof[kMaxLsqProfiles];
   LsqChannel ch[kMaxLsqChannels];
   DevProfile epl, shear;
