@@ -117,7 +117,8 @@ __device__ __forceinline__ EplGeom epl_geom(const EplC& c, float x, float y) {
 //   Re P = A_0 + b_1 cos(2a) - b_2,  Im P = b_1 sin(2a),
 //   b_n = A_n + 2 cos(2a) b_{n+1} - b_{n+2}  (n = K..1, b_{K+1} = b_{K+2} = 0),
 // Clenshaw's recurrence: 2 FP32 operations per term and one dependent FMA.
-// tab[n] = (A_n, n A_n, s_n A_n, 0), n = 0..K (A_0 = 1, s_0 = 0).
+// tab[n] = (A_n, n A_n, s_n A_n, s_n A_n), n = 0..K (A_0 = 1, s_0 = 0); the
+// repeated last entry lets two pixels' third recurrence read an aligned pair.
 __device__ __forceinline__ void epl_series_F(const EplGeom& g, const float4* __restrict__ tab, int K,
                                              float& Fx, float& Fy) {
   const float c2 = 2.f * g.Cs2;
@@ -159,14 +160,35 @@ __device__ __forceinline__ void epl_deflect_n(const EplC& c, const float4* __res
     b1[k] = 0.f;
     b2[k] = 0.f;
   }
+  if constexpr (NP == 4) {
+    // Packed FFMA2 over pixel pairs (0, 1) and (2, 3), the same roundings as
+    // the scalar loop (t - b2 as fma(b2, -1, t)): identical results.
+    const float2 neg = make_float2(-1.f, -1.f);
+    const float2 ca = make_float2(c2[0], c2[1]), cb = make_float2(c2[2], c2[3]);
+    float2 u1 = make_float2(0.f, 0.f), u2 = u1, v1 = u1, v2 = u1;
 #pragma unroll 2
-  for (int n = c.K; n >= 1; --n) {
-    const float a = tab[n].x;
+    for (int n = c.K; n >= 1; --n) {
+      const float a = tab[n].x;
+      const float2 aa = make_float2(a, a);
+      const float2 u0 = __ffma2_rn(ca, u1, __ffma2_rn(u2, neg, aa));
+      const float2 v0 = __ffma2_rn(cb, v1, __ffma2_rn(v2, neg, aa));
+      u2 = u1;
+      u1 = u0;
+      v2 = v1;
+      v1 = v0;
+    }
+    b1[0] = u1.x; b1[1] = u1.y; b2[0] = u2.x; b2[1] = u2.y;
+    b1[2] = v1.x; b1[3] = v1.y; b2[2] = v2.x; b2[3] = v2.y;
+  } else {
+#pragma unroll 2
+    for (int n = c.K; n >= 1; --n) {
+      const float a = tab[n].x;
 #pragma unroll
-    for (int k = 0; k < NP; ++k) {
-      const float b0 = fmaf(c2[k], b1[k], a - b2[k]);
-      b2[k] = b1[k];
-      b1[k] = b0;
+      for (int k = 0; k < NP; ++k) {
+        const float b0 = fmaf(c2[k], b1[k], a - b2[k]);
+        b2[k] = b1[k];
+        b1[k] = b0;
+      }
     }
   }
 #pragma unroll
@@ -205,20 +227,49 @@ __device__ __forceinline__ void epl_state_n(const EplC& c, const float4* __restr
     c2[k] = 2.f * s[k].g.Cs2;
     a1[k] = a2[k] = m1[k] = m2[k] = r1[k] = r2[k] = 0.f;
   }
+  if constexpr (NP == 2) {
+    // Packed FFMA2 (two FMAs per instruction, each rounded as fmaf): per
+    // pixel the F and H recurrences share the table pair (A_n, n A_n); the T
+    // recurrences of the two pixels share (s_n A_n, s_n A_n).  t - b2 is
+    // fma(b2, -1, t), the same rounding as the subtraction, so the results
+    // equal the scalar loop's bit for bit.
+    const float2 neg = make_float2(-1.f, -1.f);
+    const float2 cp0 = make_float2(c2[0], c2[0]), cp1 = make_float2(c2[1], c2[1]);
+    const float2 cr = make_float2(c2[0], c2[1]);
+    float2 p1 = make_float2(0.f, 0.f), p2 = p1, q1 = p1, q2 = p1, s1 = p1, s2 = p1;
 #pragma unroll 2
-  for (int n = c.K; n >= 1; --n) {
-    const float4 t = tab[n];
+    for (int n = c.K; n >= 1; --n) {
+      const float4 t = tab[n];
+      const float2 tam = make_float2(t.x, t.y), tss = make_float2(t.z, t.w);
+      const float2 p0 = __ffma2_rn(cp0, p1, __ffma2_rn(p2, neg, tam));
+      const float2 q0 = __ffma2_rn(cp1, q1, __ffma2_rn(q2, neg, tam));
+      const float2 s0 = __ffma2_rn(cr, s1, __ffma2_rn(s2, neg, tss));
+      p2 = p1;
+      p1 = p0;
+      q2 = q1;
+      q1 = q0;
+      s2 = s1;
+      s1 = s0;
+    }
+    a1[0] = p1.x; m1[0] = p1.y; a2[0] = p2.x; m2[0] = p2.y;
+    a1[1] = q1.x; m1[1] = q1.y; a2[1] = q2.x; m2[1] = q2.y;
+    r1[0] = s1.x; r1[1] = s1.y; r2[0] = s2.x; r2[1] = s2.y;
+  } else {
+#pragma unroll 2
+    for (int n = c.K; n >= 1; --n) {
+      const float4 t = tab[n];
 #pragma unroll
-    for (int k = 0; k < NP; ++k) {
-      const float a0 = fmaf(c2[k], a1[k], t.x - a2[k]);
-      const float m0 = fmaf(c2[k], m1[k], t.y - m2[k]);
-      const float r0 = fmaf(c2[k], r1[k], t.z - r2[k]);
-      a2[k] = a1[k];
-      a1[k] = a0;
-      m2[k] = m1[k];
-      m1[k] = m0;
-      r2[k] = r1[k];
-      r1[k] = r0;
+      for (int k = 0; k < NP; ++k) {
+        const float a0 = fmaf(c2[k], a1[k], t.x - a2[k]);
+        const float m0 = fmaf(c2[k], m1[k], t.y - m2[k]);
+        const float r0 = fmaf(c2[k], r1[k], t.z - r2[k]);
+        a2[k] = a1[k];
+        a1[k] = a0;
+        m2[k] = m1[k];
+        m1[k] = m0;
+        r2[k] = r1[k];
+        r1[k] = r0;
+      }
     }
   }
 #pragma unroll
@@ -270,7 +321,7 @@ __device__ __forceinline__ void epl_build_table(float4* tab, float f, float t, i
       }
     }
     const float A = carry_p * p, S = carry_s + dl;
-    if (n <= K) tab[n] = make_float4(A, (float)n * A, S * A, 0.f);
+    if (n <= K) tab[n] = make_float4(A, (float)n * A, S * A, S * A);
     carry_p *= __shfl_sync(0xffffffffu, p, 31);
     carry_s += __shfl_sync(0xffffffffu, dl, 31);
   }
