@@ -823,7 +823,7 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--traffic-per-launch", type=float, default=1464320.0,
+    ap.add_argument("--traffic-per-launch", type=float, default=1104128.0,
                     help="DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one fused launch "
                          "at 4096 chains, from an ncu capture of this workload (recorded in the JSON line)")
     ap.add_argument("--time-to-map", action="store_true")
