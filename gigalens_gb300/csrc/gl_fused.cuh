@@ -448,6 +448,7 @@ struct SampleConsts {
   EplC epl;
   float g1, g2;
   SerC ll, src;
+  SerC2 lls;   // (lens light, source) packed, families with a lens light
 };
 
 template <int FAM>
@@ -473,6 +474,7 @@ __device__ __forceinline__ SampleConsts<FAM> make_consts(const FusedArgs& a, con
   c.src = sersic_consts(pget(sx, s[0], 1.f), pget(sx, s[1], 1.f), pget(sx, s[2], 0.f),
                         pget(sx, s[3], 0.f), pget(sx, s[4], 0.f), pget(sx, s[5], 0.f),
                         pget(sx, s[6], 1.f));
+  if (T::kLensLight) c.lls = sersic_pack(c.ll, c.src);
   return c;
 }
 
@@ -491,9 +493,13 @@ static __device__ void phase_pixels_forward(const FusedArgs& a, const DevImage& 
       bx = bx - (c.g1 * g.x + c.g2 * g.y);
       by = by - (c.g2 * g.x - c.g1 * g.y);
     }
-    float img = 0.f;
-    if (T::kLensLight) img += sersic_light(c.ll, g.x, g.y);
-    img += sersic_light(c.src, bx, by);
+    float img;
+    if constexpr (T::kLensLight) {   // lens light at theta and source at beta, packed
+      const float2 r = sersic_light2(c.lls, make_float2(g.x, bx), make_float2(g.y, by));
+      img = r.x + r.y;
+    } else {
+      img = sersic_light(c.src, bx, by);
+    }
     if (isnan(img)) img = 0.f;
     sm[__float_as_int(g.z)] = img;
   };
@@ -540,6 +546,8 @@ static __device__ void phase_pixels_reverse(const FusedArgs& a, const DevImage& 
   SerAcc la, sa;
   la.zero();
   sa.zero();
+  SerAcc2 lsa;   // (lens light, source) accumulators, families with a lens light
+  lsa.zero();
   float g1b = 0.f, g2b = 0.f;
   const int total = I.nplanes * I.N * I.N;
   const float4* grid = reinterpret_cast<const float4*>(I.grid);
@@ -550,18 +558,20 @@ static __device__ void phase_pixels_reverse(const FusedArgs& a, const DevImage& 
       bx = bx - (c.g1 * xy.x + c.g2 * xy.y);
       by = by - (c.g2 * xy.x - c.g1 * xy.y);
     }
-    SerFwd lf;
-    float img = 0.f;
-    if (T::kLensLight) {
-      lf = sersic_fwd(c.ll, xy.x, xy.y);
-      img += lf.I;
+    float bxb, byb;
+    if constexpr (T::kLensLight) {   // lens light at theta and source at beta, packed
+      const SerFwd2 f = sersic_fwd2(c.lls, make_float2(xy.x, bx), make_float2(xy.y, by));
+      const float img = f.I.x + f.I.y;
+      if (isnan(img)) return;   // the reference zeroes NaN pixels: no gradient flows
+      float2 Xb, Yb;
+      sersic_reverse2(c.lls, f, gimg, lsa, Xb, Yb);
+      bxb = Xb.y;
+      byb = Yb.y;
+    } else {
+      const SerFwd sf = sersic_fwd(c.src, bx, by);
+      if (isnan(sf.I)) return;
+      sersic_reverse(c.src, sf, gimg, sa, bxb, byb);
     }
-    const SerFwd sf = sersic_fwd(c.src, bx, by);
-    img += sf.I;
-    if (isnan(img)) return;   // the reference zeroes NaN pixels: no gradient flows
-    float dummyx, dummyy, bxb, byb;
-    if (T::kLensLight) sersic_reverse(c.ll, lf, gimg, la, dummyx, dummyy);
-    sersic_reverse(c.src, sf, gimg, sa, bxb, byb);
     const float abx = -bxb, aby = -byb;   // beta = theta - sum alpha
     if (T::kShear) {
       g1b += abx * xy.x - aby * xy.y;
@@ -589,6 +599,12 @@ static __device__ void phase_pixels_reverse(const FusedArgs& a, const DevImage& 
   for (; px < total; px += kThreads) {
     const float4 g = __ldg(grid + px);
     pixel(g, sm[__float_as_int(g.z)], epl_state(c.epl, st.tab, g.x, g.y));
+  }
+  if constexpr (T::kLensLight) {
+    la.Ie = lsa.Ie.x; la.RsA = lsa.RsA.x; la.nA = lsa.nA.x; la.bnA = lsa.bnA.x; la.sq = lsa.sq.x;
+    la.isq = lsa.isq.x; la.phi = lsa.phi.x; la.cx = lsa.cx.x; la.cy = lsa.cy.x;
+    sa.Ie = lsa.Ie.y; sa.RsA = lsa.RsA.y; sa.nA = lsa.nA.y; sa.bnA = lsa.bnA.y; sa.sq = lsa.sq.y;
+    sa.isq = lsa.isq.y; sa.phi = lsa.phi.y; sa.cx = lsa.cx.y; sa.cy = lsa.cy.y;
   }
   float v[R_NACC] = {ea.phi, ea.SP, ea.SPlnR, ea.FH, ea.FT, ea.q, ea.cx, ea.cy,
                      g1b, g2b,

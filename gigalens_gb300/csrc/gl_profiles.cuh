@@ -482,6 +482,96 @@ __device__ __forceinline__ void sersic_reverse(const SerC& s, const SerFwd& f, f
 }
 
 // Per-sample chain to d/d(R_sersic, n_sersic, e1, e2, cx, cy, Ie).
+// Two Sersic profiles evaluated together on packed FP32 pairs (component x:
+// profile a, y: profile b; a pixel's lens light at theta and source at
+// beta).  Each packed operation rounds as its scalar counterpart (fused
+// multiply-adds where the scalar code contracts), the transcendentals run per
+// component: the values agree with sersic_light / sersic_fwd / sersic_reverse
+// to float32 rounding.
+struct SerC2 {
+  float2 ncx, ncy, cph, sph, nsph, sq, isq, a1, na0, nb, Ie, nbn;
+};
+__device__ __forceinline__ SerC2 sersic_pack(const SerC& a, const SerC& b) {
+  SerC2 p;
+  p.ncx = make_float2(-a.cx, -b.cx);
+  p.ncy = make_float2(-a.cy, -b.cy);
+  p.cph = make_float2(a.cph, b.cph);
+  p.sph = make_float2(a.sph, b.sph);
+  p.nsph = make_float2(-a.sph, -b.sph);
+  p.sq = make_float2(a.sq, b.sq);
+  p.isq = make_float2(a.isq, b.isq);
+  p.a1 = make_float2(a.a1, b.a1);
+  p.na0 = make_float2(-a.a0, -b.a0);
+  p.nb = make_float2(a.nb, b.nb);
+  p.Ie = make_float2(a.Ie, b.Ie);
+  p.nbn = make_float2(-a.bn, -b.bn);
+  return p;
+}
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+
+__device__ __forceinline__ float2 sersic_light2(const SerC2& s, float2 X, float2 Y) {
+  const float2 dX = __fadd2_rn(X, s.ncx), dY = __fadd2_rn(Y, s.ncy);
+  const float2 u = __ffma2_rn(s.cph, dX, __fmul2_rn(s.sph, dY));
+  const float2 v = __ffma2_rn(s.cph, dY, __fmul2_rn(s.nsph, dX));
+  const float2 xt1 = __fmul2_rn(u, s.sq), xt2 = __fmul2_rn(v, s.isq);
+  const float2 R2 = __ffma2_rn(xt1, xt1, __fmul2_rn(xt2, xt2));
+  const float2 t = __ffma2_rn(s.a1, make_float2(__log2f(R2.x), __log2f(R2.y)), s.na0);
+  const float2 e = __fmul2_rn(s.nb, __fadd2_rn(make_float2(exp2f(t.x), exp2f(t.y)), f2(-1.f)));
+  return __fmul2_rn(s.Ie, make_float2(exp2f(e.x), exp2f(e.y)));
+}
+
+struct SerFwd2 {
+  float2 dX, dY, u, v, xt1, xt2, R2, l2, rho, E, I;
+};
+struct SerAcc2 {
+  float2 Ie, RsA, nA, bnA, sq, isq, phi, cx, cy;
+  __device__ __forceinline__ void zero() {
+    Ie = RsA = nA = bnA = sq = isq = phi = cx = cy = make_float2(0.f, 0.f);
+  }
+};
+__device__ __forceinline__ SerFwd2 sersic_fwd2(const SerC2& s, float2 X, float2 Y) {
+  SerFwd2 f;
+  f.dX = __fadd2_rn(X, s.ncx);
+  f.dY = __fadd2_rn(Y, s.ncy);
+  f.u = __ffma2_rn(s.cph, f.dX, __fmul2_rn(s.sph, f.dY));
+  f.v = __ffma2_rn(s.cph, f.dY, __fmul2_rn(s.nsph, f.dX));
+  f.xt1 = __fmul2_rn(f.u, s.sq);
+  f.xt2 = __fmul2_rn(f.v, s.isq);
+  f.R2 = __ffma2_rn(f.xt1, f.xt1, __fmul2_rn(f.xt2, f.xt2));
+  f.l2 = make_float2(__log2f(f.R2.x), __log2f(f.R2.y));
+  const float2 t = __ffma2_rn(s.a1, f.l2, s.na0);
+  f.rho = make_float2(exp2f(t.x), exp2f(t.y));
+  const float2 e = __fmul2_rn(s.nb, __fadd2_rn(f.rho, f2(-1.f)));
+  f.E = make_float2(exp2f(e.x), exp2f(e.y));
+  f.I = __fmul2_rn(s.Ie, f.E);
+  return f;
+}
+__device__ __forceinline__ void sersic_reverse2(const SerC2& s, const SerFwd2& f, float Ib, SerAcc2& a,
+                                                float2& Xb, float2& Yb) {
+  const float2 ib = f2(Ib);
+  a.Ie = __ffma2_rn(ib, f.E, a.Ie);
+  const float2 rb = __fmul2_rn(ib, __fmul2_rn(s.nbn, f.I));   // adjoint of rho
+  const float2 rr = __fmul2_rn(rb, f.rho);
+  a.RsA = __fadd2_rn(a.RsA, rr);
+  const float2 lnrho = __fmul2_rn(f2(kLn2), __ffma2_rn(s.a1, f.l2, s.na0));
+  a.nA = __ffma2_rn(rr, lnrho, a.nA);
+  a.bnA = __ffma2_rn(__fmul2_rn(ib, f.I), __fadd2_rn(f.rho, f2(-1.f)), a.bnA);
+  const float2 ra = __fmul2_rn(rr, s.a1);
+  const float2 R2b = make_float2(f.R2.x > 0.f ? ra.x / f.R2.x : 0.f, f.R2.y > 0.f ? ra.y / f.R2.y : 0.f);
+  const float2 R2b2 = __fmul2_rn(f2(2.f), R2b);
+  const float2 xt1b = __fmul2_rn(R2b2, f.xt1), xt2b = __fmul2_rn(R2b2, f.xt2);
+  const float2 ub = __fmul2_rn(xt1b, s.sq), vb = __fmul2_rn(xt2b, s.isq);
+  a.sq = __ffma2_rn(xt1b, f.u, a.sq);
+  a.isq = __ffma2_rn(xt2b, f.v, a.isq);
+  const float2 dXb = __ffma2_rn(ub, s.cph, __fmul2_rn(vb, s.nsph));
+  const float2 dYb = __ffma2_rn(ub, s.sph, __fmul2_rn(vb, s.cph));
+  a.phi = __ffma2_rn(ub, f.v, __ffma2_rn(__fmul2_rn(vb, f2(-1.f)), f.u, a.phi));
+  a.cx = __ffma2_rn(dXb, f2(-1.f), a.cx);
+  a.cy = __ffma2_rn(dYb, f2(-1.f), a.cy);
+  Xb = dXb;
+  Yb = dYb;
+}
+
 __device__ __forceinline__ void sersic_chain(float Rs, float n, float e1, float e2, const SerC& s,
                                              const SerAcc& a, float out[7]) {
   float c = sqrtf(e1 * e1 + e2 * e2);
