@@ -402,30 +402,47 @@ __global__ void __launch_bounds__(NT, 512 / NT) lsq_basis_kernel(const __grid_co
 #undef GL_LSQ_CONV
 
 // pinv(G) h by cyclic Jacobi (round-robin parallel ordering), one CTA of
-// kSolveThreads per sample.  In the rotation phases thread t takes column (or
-// row) t % 64 of the pairs t / 64, t / 64 + kSolveThreads / 64, ...: no
-// runtime divisions.
-constexpr int kSolveThreads = 256;
+// kSolveThreads per sample.  A round rotates n/2 disjoint index pairs at once:
+// their rotations are computed first, then every 2x2 block of the lower
+// triangle (rows of pair P, columns of pair R) takes J_P^T B J_R in one pass
+// (the block mirrored above the diagonal), and V takes V J in the same pass.
+// A and V live in dynamic shared memory sized for n (row pitch n | 1, odd, so
+// column accesses stay conflict-free), so many samples share an SM.
+constexpr int kSolveThreads = 128;
+size_t solve_smem_bytes(int D) {
+  const int n = (D + 1) & ~1, ld = n | 1, np = n / 2;
+  return (size_t)(2 * n * ld + n + n) * 4 + (size_t)np * (np + 1) / 2 * 2;
+}
 __global__ void __launch_bounds__(kSolveThreads) lsq_solve_kernel(int bs, int D, const float* __restrict__ G,
                                                         const float* __restrict__ h, float rcond,
                                                         float* __restrict__ coeffs, int max_sweeps,
                                                         float* __restrict__ Vout, float* __restrict__ ilam,
                                                         const int* __restrict__ status) {
-  // rows padded to an odd number of floats: column accesses stay conflict-free
-  constexpr int kLd = (kMaxLsqChannels + 1) | 1;
-  __shared__ float A[kMaxLsqChannels + 1][kLd];
-  __shared__ float V[kMaxLsqChannels + 1][kLd];
+  extern __shared__ float4 solve_dyn[];
+  const int n = (D + 1) & ~1;   // even size; a padding index carries a zero row/column
+  const int ld = n | 1;
+  const int npair = n / 2;
+  const int nblk = npair * (npair + 1) / 2;
+  float* A = reinterpret_cast<float*>(solve_dyn);
+  float* V = A + n * ld;
+  float* hs = V + n * ld;
+  float* proj = hs + n;
+  unsigned char* blk = reinterpret_cast<unsigned char*>(proj + n);   // (k1, k2), k2 <= k1
   __shared__ float cs[kMaxLsqChannels / 2 + 1][2];
   __shared__ int pr[kMaxLsqChannels / 2 + 1][2];
-  __shared__ float hs[kMaxLsqChannels + 1];
   __shared__ float red[2];
-  const int n = (D + 1) & ~1;   // even size; a padding index carries a zero row/column
-  const int npair = n / 2;
+  __shared__ float wred[2][kSolveThreads / 32];
+  for (int b = threadIdx.x; b < nblk; b += kSolveThreads) {
+    int k1 = 0;
+    while ((k1 + 1) * (k1 + 2) / 2 <= b) ++k1;
+    blk[2 * b] = (unsigned char)k1;
+    blk[2 * b + 1] = (unsigned char)(b - k1 * (k1 + 1) / 2);
+  }
   for (int b = blockIdx.x; b < bs; b += gridDim.x) {
     for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
       const int i = t / n, j = t - i * n;
-      A[i][j] = (i < D && j < D) ? G[((size_t)b * D + i) * D + j] : 0.f;
-      V[i][j] = (i == j) ? 1.f : 0.f;
+      A[i * ld + j] = (i < D && j < D) ? G[((size_t)b * D + i) * D + j] : 0.f;
+      V[i * ld + j] = (i == j) ? 1.f : 0.f;
     }
     for (int t = threadIdx.x; t < n; t += blockDim.x) hs[t] = (t < D) ? h[(size_t)b * D + t] : 0.f;
     __syncthreads();
@@ -434,10 +451,9 @@ __global__ void __launch_bounds__(kSolveThreads) lsq_solve_kernel(int bs, int D,
       // convergence test: off-diagonal vs diagonal Frobenius norm (block reduction)
       {
         float off = 0.f, dg = 0.f;
-        for (int i = threadIdx.x >> 6; i < n; i += kSolveThreads / 64) {
-          const int j = threadIdx.x & 63;
-          if (j >= n) continue;
-          const float v = A[i][j] * A[i][j];
+        for (int t = threadIdx.x; t < n * n; t += kSolveThreads) {
+          const int i = t / n, j = t - i * n;
+          const float v = A[i * ld + j] * A[i * ld + j];
           if (i == j) dg += v;
           else off += v;
         }
@@ -445,7 +461,6 @@ __global__ void __launch_bounds__(kSolveThreads) lsq_solve_kernel(int bs, int D,
           off += __shfl_xor_sync(0xffffffffu, off, o);
           dg += __shfl_xor_sync(0xffffffffu, dg, o);
         }
-        __shared__ float wred[2][kSolveThreads / 32];
         if ((threadIdx.x & 31) == 0) {
           wred[0][threadIdx.x >> 5] = off;
           wred[1][threadIdx.x >> 5] = dg;
@@ -475,21 +490,23 @@ __global__ void __launch_bounds__(kSolveThreads) lsq_solve_kernel(int bs, int D,
       if (done) break;
       for (int round = 0; round < n - 1; ++round) {
         // tournament pairing: index 0 fixed, the others rotate
-        if (threadIdx.x < npair) {
-          const int k = threadIdx.x;
-          int p, q;
-          auto at = [&](int pos) { return pos == 0 ? 0 : 1 + ((pos - 1 + round) % (n - 1)); };
-          p = at(k);
-          q = at(n - 1 - k);
+        for (int k = threadIdx.x; k < npair; k += kSolveThreads) {
+          auto at = [&](int pos) {
+            if (pos == 0) return 0;
+            int v = pos - 1 + round;   // < 2 (n - 1)
+            if (v >= n - 1) v -= n - 1;
+            return 1 + v;
+          };
+          int p = at(k), q = at(n - 1 - k);
           if (p > q) {
             const int t = p;
             p = q;
             q = t;
           }
-          const float apq = A[p][q];
+          const float apq = A[p * ld + q];
           float c = 1.f, s = 0.f;
           if (fabsf(apq) > 1e-30f) {
-            const float theta = (A[q][q] - A[p][p]) / (2.f * apq);
+            const float theta = (A[q * ld + q] - A[p * ld + p]) / (2.f * apq);
             const float t = copysignf(1.f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.f));
             c = rsqrtf(t * t + 1.f);
             s = t * c;
@@ -500,29 +517,36 @@ __global__ void __launch_bounds__(kSolveThreads) lsq_solve_kernel(int bs, int D,
           pr[k][1] = q;
         }
         __syncthreads();
-        // rows: A <- J^T A
-        for (int k = threadIdx.x >> 6; k < npair; k += kSolveThreads / 64) {
-          const int j = threadIdx.x & 63;
-          if (j >= n) continue;
-          const int p = pr[k][0], q = pr[k][1];
-          const float c = cs[k][0], s = cs[k][1];
-          const float ap = A[p][j], aq = A[q][j];
-          A[p][j] = c * ap - s * aq;
-          A[q][j] = s * ap + c * aq;
-        }
-        __syncthreads();
-        // columns: A <- A J, V <- V J
-        for (int k = threadIdx.x >> 6; k < npair; k += kSolveThreads / 64) {
-          const int i = threadIdx.x & 63;
-          if (i >= n) continue;
-          const int p = pr[k][0], q = pr[k][1];
-          const float c = cs[k][0], s = cs[k][1];
-          const float ap = A[i][p], aq = A[i][q];
-          A[i][p] = c * ap - s * aq;
-          A[i][q] = s * ap + c * aq;
-          const float vp = V[i][p], vq = V[i][q];
-          V[i][p] = c * vp - s * vq;
-          V[i][q] = s * vp + c * vq;
+        // A <- J^T A J block by block (lower triangle, mirrored); V <- V J
+        for (int t = threadIdx.x; t < nblk + n * npair; t += kSolveThreads) {
+          if (t < nblk) {
+            const int k1 = blk[2 * t], k2 = blk[2 * t + 1];
+            const int p = pr[k1][0], q = pr[k1][1], r = pr[k2][0], u = pr[k2][1];
+            const float cP = cs[k1][0], sP = cs[k1][1], cR = cs[k2][0], sR = cs[k2][1];
+            const float b00 = A[p * ld + r], b01 = A[p * ld + u], b10 = A[q * ld + r], b11 = A[q * ld + u];
+            const float t00 = cP * b00 - sP * b10, t01 = cP * b01 - sP * b11;
+            const float t10 = sP * b00 + cP * b10, t11 = sP * b01 + cP * b11;
+            const float n00 = cR * t00 - sR * t01, n01 = sR * t00 + cR * t01;
+            const float n10 = cR * t10 - sR * t11, n11 = sR * t10 + cR * t11;
+            A[p * ld + r] = n00;
+            A[p * ld + u] = n01;
+            A[q * ld + r] = n10;
+            A[q * ld + u] = n11;
+            if (k1 != k2) {
+              A[r * ld + p] = n00;
+              A[u * ld + p] = n01;
+              A[r * ld + q] = n10;
+              A[u * ld + q] = n11;
+            }
+          } else {
+            const int e = t - nblk;
+            const int k = e / n, i = e - k * n;
+            const int p = pr[k][0], q = pr[k][1];
+            const float c = cs[k][0], s = cs[k][1];
+            const float vp = V[i * ld + p], vq = V[i * ld + q];
+            V[i * ld + p] = c * vp - s * vq;
+            V[i * ld + q] = s * vp + c * vq;
+          }
         }
         __syncthreads();
       }
@@ -530,17 +554,16 @@ __global__ void __launch_bounds__(kSolveThreads) lsq_solve_kernel(int bs, int D,
     // pinv solve: coeffs = sum over kept eigenpairs of (v_i . h / lambda_i) v_i
     if (threadIdx.x == 0) {
       float m = 0.f;
-      for (int i = 0; i < D; ++i) m = fmaxf(m, fabsf(A[i][i]));
+      for (int i = 0; i < D; ++i) m = fmaxf(m, fabsf(A[i * ld + i]));
       red[0] = rcond * m;
     }
     __syncthreads();
     const float cutoff = red[0];
-    // proj_i = (v_i . h) / lambda_i, reuse cs[][0] as storage when n/2 >= D is false -> use hs tail
-    __shared__ float proj[kMaxLsqChannels + 1];
+    // proj_i = (v_i . h) / lambda_i
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       float s = 0.f;
-      for (int r = 0; r < n; ++r) s = fmaf(V[r][i], hs[r], s);
-      const float lam = A[i][i];
+      for (int r = 0; r < n; ++r) s = fmaf(V[r * ld + i], hs[r], s);
+      const float lam = A[i * ld + i];
       proj[i] = (i < D && fabsf(lam) > cutoff) ? s / lam : 0.f;
     }
     __syncthreads();
@@ -548,15 +571,15 @@ __global__ void __launch_bounds__(kSolveThreads) lsq_solve_kernel(int bs, int D,
     const bool bad = status && *status;
     for (int t = threadIdx.x; t < D * D; t += blockDim.x) {
       const int r = t / D, i = t - r * D;
-      Vout[(size_t)b * D * D + t] = V[r][i];
+      Vout[(size_t)b * D * D + t] = V[r * ld + i];
     }
     for (int i = threadIdx.x; i < D; i += blockDim.x) {
-      const float lam = A[i][i];
+      const float lam = A[i * ld + i];
       ilam[(size_t)b * D + i] = fabsf(lam) > cutoff ? 1.f / lam : 0.f;
     }
     for (int r = threadIdx.x; r < D; r += blockDim.x) {
       float s = 0.f;
-      for (int i = 0; i < n; ++i) s = fmaf(V[r][i], proj[i], s);
+      for (int i = 0; i < n; ++i) s = fmaf(V[r * ld + i], proj[i], s);
       coeffs[(size_t)b * D + r] = bad ? __int_as_float(0x7fc00000) : s;
     }
     __syncthreads();
@@ -1153,8 +1176,8 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   // least-squares problem itself
   const int xpass_blocks = std::min(bs, sms);
   const size_t xsm = xpass_smem_bytes(L->D);
-  lsq_solve_kernel<<<bs < 8 * sms ? bs : 8 * sms, kSolveThreads, 0, stream>>>(bs, L->D, G, h, 1e-6f, co, 30, V,
-                                                                            ilam, status);
+  lsq_solve_kernel<<<bs < 12 * sms ? bs : 12 * sms, kSolveThreads, solve_smem_bytes(L->D), stream>>>(
+      bs, L->D, G, h, 1e-6f, co, 30, V, ilam, status);
   for (int it = 0; it < 2; ++it) {
     lsq_xpass_kernel<false><<<xpass_blocks, kXT, xsm, stream>>>(a, co, r, nullptr, nullptr, nullptr);
     lsq_update_kernel<<<bs < 8 * sms ? bs : 8 * sms, 64, 0, stream>>>(bs, L->D, V, ilam, r, co);
