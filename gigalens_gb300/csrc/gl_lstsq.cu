@@ -62,6 +62,33 @@ __device__ __forceinline__ void hermite_fn_n(int n, const float (&u)[U], float (
   float tu[U];
 #pragma unroll
   for (int k = 0; k < U; ++k) tu[k] = 2.f * u[k];
+  if constexpr (U % 2 == 0) {
+    // pixel pairs on packed FP32 (FMUL2, FFMA2): the same roundings as the
+    // scalar step, so the values are identical
+    float2 p0[U / 2], p1[U / 2], pt[U / 2];
+#pragma unroll
+    for (int k = 0; k < U / 2; ++k) {
+      p0[k] = make_float2(h0[2 * k], h0[2 * k + 1]);
+      p1[k] = make_float2(h1[2 * k], h1[2 * k + 1]);
+      pt[k] = make_float2(tu[2 * k], tu[2 * k + 1]);
+    }
+    for (int i = 2; i <= n; ++i) {
+      const float c2 = -(float)(2 * (i - 1));
+      const float2 nc = make_float2(c2, c2);
+#pragma unroll
+      for (int k = 0; k < U / 2; ++k) {
+        const float2 h2 = __ffma2_rn(pt[k], p1[k], __fmul2_rn(nc, p0[k]));
+        p0[k] = p1[k];
+        p1[k] = h2;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < U / 2; ++k) {
+      out[2 * k] = p1[k].x * pref[n];
+      out[2 * k + 1] = p1[k].y * pref[n];
+    }
+    return;
+  }
   for (int i = 2; i <= n; ++i) {
     const float c2 = (float)(2 * (i - 1));
 #pragma unroll
