@@ -630,13 +630,13 @@ __global__ void __launch_bounds__(kSolveThreads) lsq_solve_kernel(int bs, int D,
 //         the Gaussian log-likelihood with the data error map and chi^2
 //         (BackwardProbModel, tf/model.py:157-163).
 constexpr int kXT = 256;      // threads = pixels per chunk
-constexpr int kXRing = 3;     // chunks in the ring
+constexpr int kXRing = 2;     // chunks in the ring (two blocks per SM: their chunk barriers interleave)
 constexpr int kXChPerWarp = (kMaxLsqChannels + (kXT / 32) - 1) / (kXT / 32);
 
 size_t xpass_smem_bytes(int D) { return (size_t)kXRing * D * kXT * 4; }
 
 template <bool IMAGE>
-__global__ void __launch_bounds__(kXT, 1) lsq_xpass_kernel(const __grid_constant__ LsqArgs a,
+__global__ void __launch_bounds__(kXT, 2) lsq_xpass_kernel(const __grid_constant__ LsqArgs a,
                                                           const float* __restrict__ coeffs,
                                                           float* __restrict__ r_out, float* img_out,
                                                           float* logL, float* chi2) {
@@ -1201,7 +1201,7 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   if (rc) return rc;
   // c0 = pinv(G) h, then two refinement steps against the residual of the
   // least-squares problem itself
-  const int xpass_blocks = std::min(bs, sms);
+  const int xpass_blocks = std::min(bs, 2 * sms);
   const size_t xsm = xpass_smem_bytes(L->D);
   lsq_solve_kernel<<<bs < 12 * sms ? bs : 12 * sms, kSolveThreads, solve_smem_bytes(L->D), stream>>>(
       bs, L->D, G, h, 1e-6f, co, 30, V, ilam, status);
