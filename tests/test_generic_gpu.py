@@ -206,6 +206,32 @@ def test_general_path_loglik_grad(name):
     _check_grad(grad, (g, band), max_rel=GRAD_LIMITS.get(name, 1e-2))
 
 
+@pytest.mark.parametrize("name", ["sie_shear_se_se", "sis_shear_se_se"])
+def test_signature_global_planes(name):
+    """The compiled signatures' global-plane kernels: 100x100 px planes exceed
+    shared memory (likelihood, chi^2 and gradient against the oracle)."""
+    s = _setup(name, num_pix=100, bs=4, seed=1)
+    plan = s["sim"].prob_plan(s["pm"])
+    x = flat_from_struct(s["x_struct"]).float().cuda().contiguous()
+    bs = x.shape[0]
+    cfg = plan.launch_config(bs)
+    assert cfg["family"] == CASE_FAMILY[name] and cfg["global_planes"] == 1
+    logL = torch.empty(bs, device="cuda")
+    chi2 = torch.empty(bs, device="cuda")
+    grad = torch.empty_like(x)
+    N.call("gl_forward_grad", plan.handle, N.ptr(x), None, bs, N.ptr(logL), N.ptr(chi2), N.ptr(grad), None,
+           N.stream_ptr())
+    torch.cuda.synchronize()
+    x64 = x.double().cpu().requires_grad_(True)
+    ll, c2 = O.forward_log_likelihood_flat(s["om"], s["ocfg"], x64, s["obs"].astype(np.float64), 0.2, 1000.0)
+    (g,) = torch.autograd.grad(ll.sum(), x64)
+    band = fp32_band(lambda xx: O.forward_log_likelihood_flat(s["om"], s["ocfg"], xx, s["obs"], 0.2, 1000.0,
+                                                              dtype=torch.float32)[0], x.cpu(), g)
+    _check_scalar(logL, ll.detach(), 1e-4, name="logL")
+    _check_scalar(chi2, c2.detach(), 1e-4, name="chi2")
+    _check_grad(grad, (g, band), max_rel=GRAD_LIMITS.get(name, 1e-2))
+
+
 def test_general_path_log_prob_autograd():
     """ForwardProbModel.log_prob on the general path (prior + bijector in the kernel)."""
     s = _setup("sie_shear_coresersic_se", bs=5, seed=3)
