@@ -263,8 +263,8 @@ def lstsq_flops(n, D=45, ss=2, k=21):
     basis: 110 flop per supersampled pixel (coordinates, Hermite recursions,
     the D products); psf: the PSF + binning of every channel, D strided
     correlations with the (k+ss-1)^2 combined kernel at the n^2 outputs;
-    gram: A^T W A, 2 n^2 D(D+1)/2 (run as three TF32 tensor-core products,
-    counted once); rhs: A^T W b, 2 n^2 D."""
+    gram: A^T W A, 2 n^2 D(D+1)/2 (counted once also where the tensor-core
+    variant runs it as three TF32 products); rhs: A^T W b, 2 n^2 D."""
     P, Ps, kc = n * n, (ss * n) ** 2, k + ss - 1
     return {"basis": 110.0 * Ps, "psf": D * 2.0 * P * kc * kc,
             "gram": 2.0 * P * D * (D + 1) / 2, "rhs": 2.0 * P * D}
@@ -305,7 +305,8 @@ def lstsq_workload(torch, dev, n_big=2048, n_small=512, tuning=None):
     img_id = torch.cat([torch.zeros(n_big, dtype=torch.int32), torch.ones(n_small, dtype=torch.int32)]).to(dev)
     from gigalens_gb300.cuda import autotune
     if tuning:   # a fixed launch shape instead of the tuner's choice
-        autotune.set_tuning(lplan, lsq_ctas_per_sm=tuning[0], lsq_col_block=tuning[1])
+        autotune.set_tuning(lplan, lsq_ctas_per_sm=tuning[0], lsq_col_block=tuning[1],
+                            lsq_gram=tuning[2] if len(tuning) > 2 else 0)
     else:        # the tuner's choice (timed on these inputs on first use, then cached)
         autotune.ensure_lstsq(lplan, x, img_id)
     wb, D = ctypes.c_size_t(0), ctypes.c_int(0)
@@ -330,7 +331,8 @@ def run_lstsq_only(args):
 
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    tuning = (args.lstsq_ctas, args.lstsq_cb) if (args.lstsq_ctas or args.lstsq_cb) else None
+    tuning = ((args.lstsq_ctas, args.lstsq_cb, args.lstsq_gram)
+              if (args.lstsq_ctas or args.lstsq_cb or args.lstsq_gram) else None)
     lsq, nb, wb, work = lstsq_workload(torch, dev, args.lstsq_big, args.lstsq_small, tuning)
     for _ in range(args.warmup):
         lsq()
@@ -833,6 +835,8 @@ def main():
     ap.add_argument("--lstsq-small", type=int, default=512, help="samples of the 60x60 image")
     ap.add_argument("--lstsq-ctas", type=int, default=0, help="basis kernel CTAs per SM (1 or 2; 0: plan default)")
     ap.add_argument("--lstsq-cb", type=int, default=0, help="basis correlation column block (16, 20; 0: planner)")
+    ap.add_argument("--lstsq-gram", type=int, default=0,
+                    help="Gram kernel: 1 tcgen05 3xTF32, 2 FP32 register tiles (0: plan default)")
     ap.add_argument("--general-path", action="store_true",
                     help="time the general-path kernels (compiled signatures and run-time dispatch) beside the "
                          "headline family")

@@ -96,7 +96,8 @@ class gl_tune_result(ctypes.Structure):
 
 class gl_tuning(ctypes.Structure):
     _fields_ = [("lsq_ctas_per_sm", ctypes.c_int), ("lsq_col_block", ctypes.c_int),
-                ("fused_corr", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("fused_corr", ctypes.c_int), ("lsq_gram", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
 
 
 class gl_image_desc(ctypes.Structure):

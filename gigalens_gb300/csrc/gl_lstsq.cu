@@ -950,6 +950,7 @@ int lsq_plan_layout(LsqPlan* L, const gl_plan* plan, int ctas_per_sm, int col_bl
 int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs) {
   LsqPlan* L = new LsqPlan;
   memset(L, 0, sizeof(*L));
+  L->gram = 2;
   const gl_model_desc& m = plan->model;
   int D = 0;
   for (int i = 0; i < m.n_profiles; ++i) {
@@ -1191,13 +1192,17 @@ int lsq_run(const gl_plan* plan, const float* x, const int* img_id, int bs, floa
   int sms = 1;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
   cudaMemsetAsync(status, 0, sizeof(int), stream);
-  // basis stack, then G = A^T A and h = A^T b on the tensor cores (3xTF32)
+  // basis stack, then G = A^T A and h = A^T b (FP32 register tiles, or the
+  // tensor cores in 3xTF32)
   if (L->nt == 512)
     lsq_basis_kernel<512><<<n_basis, 512, L->smem_bytes, stream>>>(a);
   else
     lsq_basis_kernel<256><<<n_basis, 256, L->smem_bytes, stream>>>(a);
-  const int gram_grid = std::min(bs, gram_tc_ctas_per_sm(L->D) * sms);
-  int rc = launch_gram_tc(a, G, h, status, gram_grid, stream);
+  int rc;
+  if (L->gram == 1)
+    rc = launch_gram_tc(a, G, h, status, std::min(bs, gram_tc_ctas_per_sm(L->D) * sms), stream);
+  else
+    rc = launch_gram_fp32(a, G, h, std::min(bs, sms), stream);
   if (rc) return rc;
   // c0 = pinv(G) h, then two refinement steps against the residual of the
   // least-squares problem itself
@@ -1339,7 +1344,12 @@ extern "C" int gl_plan_set_tuning(gl_plan* plan, const gl_tuning* t) {
     set_error("gl_plan_set_tuning: fused_corr %d (1 FFMA2, 2 scalar FFMA)", t->fused_corr);
     return GL_ERR_INVALID;
   }
+  if (t->lsq_gram < 0 || t->lsq_gram > 2) {
+    set_error("gl_plan_set_tuning: lsq_gram %d (1 tensor cores, 2 FP32)", t->lsq_gram);
+    return GL_ERR_INVALID;
+  }
   if (t->fused_corr) plan->corr_scalar = t->fused_corr == 2;
+  if (plan->lsq && t->lsq_gram) ((LsqPlan*)plan->lsq)->gram = t->lsq_gram;
   if (!plan->lsq || (t->lsq_ctas_per_sm == 0 && t->lsq_col_block == 0)) return GL_OK;
   LsqPlan* L = (LsqPlan*)plan->lsq;
   const int ctas = t->lsq_ctas_per_sm ? t->lsq_ctas_per_sm : L->ctas_per_sm;
@@ -1368,6 +1378,7 @@ extern "C" int gl_plan_get_tuning(const gl_plan* plan, gl_tuning* t) {
     const LsqPlan* L = (const LsqPlan*)plan->lsq;
     t->lsq_ctas_per_sm = L->ctas_per_sm;
     t->lsq_col_block = L->img[0].CB;
+    t->lsq_gram = L->gram;
   }
   return GL_OK;
 }

@@ -72,6 +72,7 @@ struct LsqPlan {
   int n_sm;             // CTAs of the basis kernel at most (ctas_per_sm per SM)
   int nt, ctas_per_sm;  // basis kernel: threads per CTA (512 or 256) and CTAs per SM
   int col_block;        // forced correlation column block (0: planner's choice)
+  int gram;             // Gram kernel: 1 tensor cores (3xTF32), 2 FP32 register tiles
   size_t beta_per_cta;  // float2 of the largest band's ray-traced coordinates (and Gaussian factors)
   int gfac_prof;        // see LsqArgs
   LsqProfile prof[kMaxLsqProfiles];
@@ -88,6 +89,9 @@ int launch_gram_tc(const LsqArgs& a, float* G, float* h, int* status, int grid, 
 int gram_tc_smem_bytes(int D);
 int gram_tc_ctas_per_sm(int D);
 void set_gram_wait_polls(int polls);   // < 0: the default limit
+// FP32 register-tile Gram (gl_gram_fp32.cu): same G and h, no wait or status
+int launch_gram_fp32(const LsqArgs& a, float* G, float* h, int grid, cudaStream_t stream);
+int gram_fp32_smem_bytes(int D);
 size_t lsq_status_offset(const LsqPlan* L, int bs);
 void lsq_destroy(gl_plan* plan);
 size_t lsq_workspace_bytes(const LsqPlan* L, int bs);

@@ -80,12 +80,13 @@ def clear_memory_cache():
 def get_tuning(plan) -> dict:
     t = N.gl_tuning()
     N.call("gl_plan_get_tuning", plan.handle, ctypes.byref(t))
-    return {"lsq_ctas_per_sm": t.lsq_ctas_per_sm, "lsq_col_block": t.lsq_col_block, "fused_corr": t.fused_corr}
+    return {"lsq_ctas_per_sm": t.lsq_ctas_per_sm, "lsq_col_block": t.lsq_col_block, "fused_corr": t.fused_corr,
+            "lsq_gram": t.lsq_gram}
 
 
-def set_tuning(plan, lsq_ctas_per_sm=0, lsq_col_block=0, fused_corr=0):
+def set_tuning(plan, lsq_ctas_per_sm=0, lsq_col_block=0, fused_corr=0, lsq_gram=0):
     t = N.gl_tuning(lsq_ctas_per_sm=int(lsq_ctas_per_sm), lsq_col_block=int(lsq_col_block),
-                    fused_corr=int(fused_corr))
+                    fused_corr=int(fused_corr), lsq_gram=int(lsq_gram))
     N.call("gl_plan_set_tuning", plan.handle, ctypes.byref(t))
 
 
@@ -189,6 +190,10 @@ def ensure_lstsq(plan, x: torch.Tensor, img_id=None, reps: int = 3):
         bench.bufs = {}
         cands = [dict(lsq_ctas_per_sm=c, lsq_col_block=cb) for c in (1, 2) for cb in (-1, 16, 20)]
         choice = _choose(plan, key, cands, bench, reps)
+        if choice is not None:
+            # the Gram kernel reads the basis stack the basis kernel wrote, whatever its
+            # shape: time its two variants on the chosen basis shape
+            choice = _choose(plan, key, [dict(choice, lsq_gram=g) for g in (2, 1)], bench, reps)
         plan._tuned_lstsq = True
         return choice
 

@@ -312,12 +312,16 @@ int gl_autotune(const gl_plan* plan, int bs, gl_tune_result* out);
  *   fused_corr       the fused kernel's PSF correlations (EPL + shear +
  *                    Sersic lens light + Sersic source, image planes in
  *                    shared memory): 1 packed FFMA2, 2 scalar FFMA; other
- *                    models always use FFMA2                              */
+ *                    models always use FFMA2
+ *   lsq_gram         the normal equations A^T A, A^T b: 1 tcgen05 tensor
+ *                    cores in 3xTF32 (its pipeline waits are bounded and set
+ *                    the status word), 2 FP32 register tiles (the default)  */
 typedef struct {
   int lsq_ctas_per_sm;
   int lsq_col_block;
   int fused_corr;
-  int reserved[5];
+  int lsq_gram;
+  int reserved[4];
 } gl_tuning;
 int gl_plan_set_tuning(gl_plan* plan, const gl_tuning* t);
 int gl_plan_get_tuning(const gl_plan* plan, gl_tuning* t);

@@ -157,7 +157,10 @@ def _lstsq(plan, x, work, nb, D):
 
 
 def test_gram_wait_timeout_returns_status_and_nan_then_recovers():
+    from gigalens_gb300.cuda import autotune
+
     plan, x = _lstsq_case()
+    autotune.set_tuning(plan, lsq_gram=1)   # the tensor-core Gram, whose pipeline waits are bounded
     bs = x.shape[0]
     nb, D = ctypes.c_size_t(0), ctypes.c_int(0)
     N.call("gl_lstsq_workspace", plan.handle, bs, ctypes.byref(nb), ctypes.byref(D))

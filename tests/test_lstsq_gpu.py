@@ -201,15 +201,21 @@ def test_lstsq_interpolated_shapelets_match_oracle():
     assert float(((ref_exact - ref).abs() / scale).max()) > 1e-3
 
 
-def test_tensor_core_gram_accuracy():
-    """G = A^T A from the tcgen05 3xTF32 kernel against float64 from the same
-    basis stack (both read from the workspace: X first, then G).  3xTF32
-    keeps about 21 bits per product and the tensor core sums in FP32 within
-    each 1024-pixel segment (segments are summed in FP64): ~5e-6 of max|G|."""
+@pytest.mark.parametrize("gram", [1, 2])
+def test_gram_accuracy(gram, monkeypatch):
+    """G = A^T A against float64 from the same basis stack (both read from
+    the workspace: X first, then G), for both Gram kernels.  1: tcgen05
+    3xTF32, which keeps about 21 bits per product and sums in FP32 within
+    each 1024-pixel segment (segments in float-float): ~5e-6 of max|G|.
+    2: FP32 register tiles, each thread summing its pixel range in FP32 and
+    the ranges added in a fixed order."""
     import ctypes
 
     from gigalens_gb300 import _native as N
+    from gigalens_gb300.cuda import autotune
     from gigalens_gb300.cuda.simulator import LensSimulator
+
+    monkeypatch.setenv("GIGALENS_GB300_AUTOTUNE", "0")   # keep the variant set below
 
     n, n_max = 40, 8
     prior = shapelet_prior(n_max, True)
@@ -221,6 +227,8 @@ def test_tensor_core_gram_accuracy():
     bs = 5
     sim = LensSimulator(phys, cfg, bs=bs)
     plan = sim.lstsq_plan(obs, err)
+    autotune.set_tuning(plan, lsq_gram=gram)
+    assert autotune.get_tuning(plan)["lsq_gram"] == gram
     x = sim.layout.flatten_params(prior.sample(bs, seed=3))
     r = sim.run_lstsq(plan, x, want_image=False)
     torch.cuda.synchronize()
@@ -233,5 +241,43 @@ def test_tensor_core_gram_accuracy():
     A = X / torch.as_tensor(err.reshape(-1), dtype=torch.float64)
     G64 = A @ A.transpose(1, 2)
     rel = float(((G - G64).abs() / G64.abs().amax(dim=(1, 2), keepdim=True)).max())
+    print("\n[Gram variant %d] max |G - G64| / max|G64| = %.2e" % (gram, rel))
     assert rel < 2e-5, rel
+    assert torch.equal(G, G.transpose(1, 2))
     assert bool(torch.isfinite(r["coeffs"]).all())
+
+
+def test_gram_variants_agree_on_the_solution(monkeypatch):
+    """The full least-squares call (37 samples of a 60x60 image, 45 shapelet
+    channels) with either Gram kernel: the same images and likelihoods to
+    the accuracy the refinement passes leave, and the FP32 kernel bitwise
+    reproducible."""
+    from gigalens_gb300 import _native as N
+    from gigalens_gb300.cuda import autotune
+    from gigalens_gb300.cuda.simulator import LensSimulator
+
+    monkeypatch.setenv("GIGALENS_GB300_AUTOTUNE", "0")
+    n, n_max = 60, 8
+    prior = shapelet_prior(n_max)
+    phys, _ = models(n_max, False)
+    cfg = SimulatorConfig(delta_pix=0.08, num_pix=n, supersample=2, kernel_supersampled=gaussian_psf(0.1, 0.04, 21))
+    obs = _obs(n, np.random.default_rng(11))
+    err = np.sqrt(0.1 ** 2 + np.clip(obs, 0, None) / 200.0).astype(np.float32)
+    bs = 37
+    sim = LensSimulator(phys, cfg, bs=bs)
+    plan = sim.lstsq_plan(obs, err)
+    x = sim.layout.flatten_params(prior.sample(bs, seed=5))
+    out = {}
+    for g in (1, 2, 2):
+        autotune.set_tuning(plan, lsq_gram=g)
+        r = sim.run_lstsq(plan, x, want_image=True, want_loglik=True)
+        torch.cuda.synchronize()
+        out.setdefault(g, []).append((r["img"].clone(), r["logL"].clone(), r["coeffs"].clone()))
+    (i1, l1, _), = out[1]
+    (i2, l2, c2), (i2b, l2b, c2b) = out[2]
+    assert torch.equal(c2, c2b) and torch.equal(i2, i2b) and torch.equal(l2, l2b)
+    rel = float(((i1 - i2).abs() / i1.abs().amax(dim=1, keepdim=True)).max())
+    print("\n[Gram variants] image max |d|/max %.2e, logL max rel %.2e"
+          % (rel, float(((l1 - l2).abs() / l1.abs()).max())))
+    assert rel < 1e-5
+    assert torch.allclose(l1, l2, rtol=1e-5)
