@@ -128,8 +128,9 @@ def _time_ms(fn, reps: int, warmup: int = 2) -> float:
     return times[len(times) // 2]
 
 
-def _choose(plan, key, candidates, bench, reps):
-    """Time every candidate (a dict of set_tuning arguments), apply and cache the fastest."""
+def _choose(plan, key, candidates, bench, reps, count=True):
+    """Time every candidate (a dict of set_tuning arguments), apply and cache the
+    fastest.  ``count``: add one to ``stats["timed"]`` (one per tuned plan shape)."""
     results = []
     for cand in candidates:
         try:
@@ -146,7 +147,8 @@ def _choose(plan, key, candidates, bench, reps):
     best_ms, best = results[0]
     set_tuning(plan, **best)
     _store(key, {"choice": best, "ms": best_ms, "timings": [[ms, c] for ms, c in results]})
-    stats["timed"] += 1
+    if count:
+        stats["timed"] += 1
     return best
 
 
@@ -193,7 +195,7 @@ def ensure_lstsq(plan, x: torch.Tensor, img_id=None, reps: int = 3):
         if choice is not None:
             # the Gram kernel reads the basis stack the basis kernel wrote, whatever its
             # shape: time its two variants on the chosen basis shape
-            choice = _choose(plan, key, [dict(choice, lsq_gram=g) for g in (2, 1)], bench, reps)
+            choice = _choose(plan, key, [dict(choice, lsq_gram=g) for g in (2, 1)], bench, reps, count=False)
         plan._tuned_lstsq = True
         return choice
 

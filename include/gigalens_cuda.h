@@ -259,9 +259,10 @@ int gl_lstsq_noalloc(const gl_plan* plan, const float* x, const int* img_id, int
 
 /* Status word of the last gl_lstsq / gl_lstsq_noalloc call of bs chains on
  * this plan (no reference counterpart: TF raises no error for this).  The
- * Gram kernel's waits on the tensor cores are bounded; a wait that runs out
- * sets the word to 1, the kernel drains its MMAs, frees its tensor memory and
- * returns, and the solve writes NaN coefficients.  work: the workspace given
+ * tensor-core Gram kernel's waits (gl_tuning.lsq_gram = 1) are bounded; a
+ * wait that runs out sets the word to 1, the kernel drains its MMAs, frees
+ * its tensor memory and returns, and the solve writes NaN coefficients.  The
+ * default FP32 Gram kernel has no waits and leaves the word 0.  work: the workspace given
  * to gl_lstsq, or NULL for gl_lstsq_noalloc's fixed scratch.  *status
  * (device or host memory) receives the word, stream-ordered: 0 = ok.       */
 int gl_lstsq_status(const gl_plan* plan, int bs, const void* work, int* status, void* stream);
