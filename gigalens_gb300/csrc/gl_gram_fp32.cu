@@ -187,11 +187,12 @@ __global__ void __launch_bounds__(kFT, 1) lsq_gram_fp32_kernel(const __grid_cons
           for (int s = 0; s < 8; ++s) {
             const float4 xj = *reinterpret_cast<const float4*>(pj + s * NT * S::pitch);
             const float2 j01 = make_float2(xj.x, xj.y), j23 = make_float2(xj.z, xj.w);
+            // pixels 0-1 of the quad into the column's eight accumulators, then
+            // pixels 2-3: eight independent FFMA2 between dependent ones
 #pragma unroll
-            for (int r = 0; r < 8; ++r) {
-              acc[r][s] = __ffma2_rn(make_float2(xi[r].x, xi[r].y), j01, acc[r][s]);
-              acc[r][s] = __ffma2_rn(make_float2(xi[r].z, xi[r].w), j23, acc[r][s]);
-            }
+            for (int r = 0; r < 8; ++r) acc[r][s] = __ffma2_rn(make_float2(xi[r].x, xi[r].y), j01, acc[r][s]);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) acc[r][s] = __ffma2_rn(make_float2(xi[r].z, xi[r].w), j23, acc[r][s]);
           }
         }
       }
