@@ -229,6 +229,9 @@ def test_gram_accuracy(gram, monkeypatch):
     plan = sim.lstsq_plan(obs, err)
     autotune.set_tuning(plan, lsq_gram=gram)
     assert autotune.get_tuning(plan)["lsq_gram"] == gram
+    with pytest.raises(N.GigaLensCudaError):
+        autotune.set_tuning(plan, lsq_gram=3)   # rejected, the plan keeps its variant
+    assert autotune.get_tuning(plan)["lsq_gram"] == gram
     x = sim.layout.flatten_params(prior.sample(bs, seed=3))
     r = sim.run_lstsq(plan, x, want_image=False)
     torch.cuda.synchronize()
