@@ -246,20 +246,6 @@ static int launch_nt(const LsqArgs& a, float* G, float* h, int grid, cudaStream_
   return GL_OK;
 }
 
-int gram_fp32_smem_bytes(int D) {
-  switch ((D + 8) / 8) {
-    case 1: return GShape<1>::smem_bytes;
-    case 2: return GShape<2>::smem_bytes;
-    case 3: return GShape<3>::smem_bytes;
-    case 4: return GShape<4>::smem_bytes;
-    case 5: return GShape<5>::smem_bytes;
-    case 6: return GShape<6>::smem_bytes;
-    case 7: return GShape<7>::smem_bytes;
-    case 8: return GShape<8>::smem_bytes;
-    default: return -1;
-  }
-}
-
 int launch_gram_fp32(const LsqArgs& a, float* G, float* h, int grid, cudaStream_t stream) {
   switch ((a.D + 8) / 8) {   // NT = ceil((D + 1) / 8)
     case 1: return launch_nt<1>(a, G, h, grid, stream);

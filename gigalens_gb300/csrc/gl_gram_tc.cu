@@ -333,8 +333,6 @@ __global__ void __launch_bounds__(kGT, 1) lsq_gram_tc_kernel(const __grid_consta
   if (warp == 0) tc_dealloc(tmem, kTmemCols);
 }
 
-int gram_tc_smem_bytes(int D) { return gram_smem_bytes(D + 1); }
-
 int gram_tc_ctas_per_sm(int) { return 1; }
 
 int launch_gram_tc(const LsqArgs& a, float* G, float* h, int* status, int grid, cudaStream_t stream) {

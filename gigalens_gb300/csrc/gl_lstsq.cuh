@@ -86,12 +86,10 @@ int lsq_prepare(gl_plan* plan, std::vector<std::vector<float>>& errs);
 int lsq_plan_layout(LsqPlan* L, const gl_plan* plan, int ctas_per_sm, int col_block);
 // tensor-core Gram (gl_gram_tc.cu)
 int launch_gram_tc(const LsqArgs& a, float* G, float* h, int* status, int grid, cudaStream_t stream);
-int gram_tc_smem_bytes(int D);
 int gram_tc_ctas_per_sm(int D);
 void set_gram_wait_polls(int polls);   // < 0: the default limit
 // FP32 register-tile Gram (gl_gram_fp32.cu): same G and h, no wait or status
 int launch_gram_fp32(const LsqArgs& a, float* G, float* h, int grid, cudaStream_t stream);
-int gram_fp32_smem_bytes(int D);
 size_t lsq_status_offset(const LsqPlan* L, int bs);
 void lsq_destroy(gl_plan* plan);
 size_t lsq_workspace_bytes(const LsqPlan* L, int bs);
