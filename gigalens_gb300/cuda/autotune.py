@@ -8,7 +8,9 @@ plan's tunable launch shapes (``gl_tuning`` in the C ABI) are:
   memory): packed FFMA2 or scalar FFMA;
 * the least-squares basis kernel: one CTA of 512 threads per SM on
   whole-image parity planes, or two CTAs of 256 threads on row bands; and
-  its correlation column block (16 or 20 outputs per lane).
+  its correlation column block (16 or 20 outputs per lane);
+* the least-squares Gram kernel: FP32 register tiles or tcgen05 3xTF32,
+  timed on the basis shape chosen first.
 
 On the first call for a plan shape (images, PSF sizes, model, basis
 channels, batch size rounded up to a power of two, SM count and GPU name)
